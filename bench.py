@@ -1,0 +1,391 @@
+"""Benchmark: batched SSE sweeps on GB300.
+
+Workload (the batched uniform configuration): 4096 independent walkers of the
+S=1/2 antiferromagnetic Heisenberg model on a 32x32 periodic square lattice
+(2048 bonds) at beta = 16, per-walker Philox streams, 2000 thermalisation
+sweeps, then measured sweeps (Carlo.sweep! + Carlo.measure!).  A "step" is
+one sweep block: `--sweeps-per-step` Carlo steps of every walker in one
+persistent launch.  Inputs are synthetic (generated models, seeded chains).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W]
+  python bench.py --impl reference     # the CPU implementation of the path on the host cores
+
+Prints one JSON line.  `value` is whole-job walker-sweeps/s from CUDA events
+around the sweep launches (walker state resident in HBM); `e2e` is the same
+metric through the public API per step (ids H2D, sweep, observables D2H),
+wall-clock.  `roofline` relates the algorithmic bytes of the sweep kernel
+(28 L + 12 W + 8 N per walker-sweep) to the measured HBM copy bandwidth.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+import _sse_loader  # noqa: E402
+
+WORKLOAD = "4096 walkers, S=1/2 Heisenberg, 32x32 periodic square (2048 bonds), beta=16"
+METRIC = "walker-sweeps/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--walkers", type=int, default=4096)
+    ap.add_argument("--side", type=int, default=32)
+    ap.add_argument("--beta", type=float, default=16.0)
+    ap.add_argument("--therm", type=int, default=2000, help="thermalisation sweeps before the warm-up steps")
+    ap.add_argument("--sweeps-per-step", type=int, default=20)
+    ap.add_argument("--plain-walkers", type=int, default=8)
+    ap.add_argument("--cpu-sweeps", type=int, default=20, help="sweeps per chain in the CPU baseline sample")
+    ap.add_argument("--cpu-threads", type=int, default=0)
+    ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--profile", action="store_true", help="open a profiler range around the timed steps only")
+    return ap.parse_args()
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_model(S, side):
+    return S.MagnetModel({"lattice": {"unitcell": S.UnitCells.square, "size": (side, side)}, "J": 1.0,
+                          "measure": ["magnetization", "staggered_magnetization"]})
+
+
+def walker_bytes(L, W, N):
+    """Algorithmic DRAM bytes of one walker-sweep: diagonal update r+w 4L, linking r 4L + w 16L,
+    slot index w 4L, worm 12 B per step (link r, opcode r+w), state r+w 4N+4N."""
+    return 28.0 * L + 12.0 * W + 8.0 * N
+
+
+def dist_setup(args):
+    rank, world, local = 0, 1, 0
+    if "RANK" in os.environ and int(os.environ.get("WORLD_SIZE", "1")) > 1:
+        import torch.distributed as dist
+
+        rank = int(os.environ["RANK"])
+        world = int(os.environ["WORLD_SIZE"])
+        local = int(os.environ.get("LOCAL_RANK", rank))
+        dist.init_process_group("gloo")
+    return rank, world, local
+
+
+def barrier_max(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier_sum(world, x):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def cpu_baseline(S, flat, states, args, nthreads):
+    """The CPU restatement (oracle) timed on the host cores, one chain per thread, started from
+    GPU-thermalised walker states so that it runs the same opstring lengths."""
+    from oracle import oracle as O
+
+    om = O.OracleModel(flat)
+    walkers = []
+    for k, (ops, st, inf) in enumerate(states[:nthreads]):
+        w = O.OracleWalker(om, T=1.0 / args.beta, seed=args.seed, stream=k, thermalization=0)
+        w.set_opstring(ops, inf["num_operators"])
+        w.set_state(st)
+        w.w.ctr = inf["rng_counter"]
+        w.w.num_worms = inf["num_worms"]
+        w.w.avg_worm_length = inf["avg_worm_length"]
+        w.w.sweeps = 1
+        walkers.append(w)
+    t0 = time.perf_counter()
+    O.run_parallel(om, walkers, args.cpu_sweeps, measure=True, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    ws = len(walkers) * args.cpu_sweeps
+    steps = sum(w.w.worm_steps_total for w in walkers)
+    slots = sum(w.w.slot_visits_total for w in walkers)
+    return {
+        "value": ws / dt,
+        "unit": METRIC,
+        "cores": nthreads,
+        "kind": "port",
+        "sample": f"{len(walkers)} chains x {args.cpu_sweeps} measured sweeps of the same workload from GPU-thermalised states, one chain per host thread",
+        "operator_updates_per_s": (steps + slots) / dt,
+        "seconds": dt,
+    }
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path (the oracle restatement of the
+    reference's sweep; Julia is not available to run the reference itself) on all host cores."""
+    rank, world, _ = dist_setup(args)
+    if rank != 0:
+        return
+    S = _sse_loader.load()
+    from oracle import oracle as O
+
+    flat = S.flatten_model(make_model(S, args.side))
+    om = O.OracleModel(flat)
+    nthreads = args.cpu_threads or os.cpu_count() or 1
+    walkers = [O.OracleWalker(om, T=1.0 / args.beta, seed=args.seed, stream=k, thermalization=10**9) for k in range(nthreads)]
+    for w in walkers:
+        w.init()
+    # bounded thermalisation: opstring lengths and worm counts near their working values
+    O.run_parallel(om, walkers, 300, measure=False, nthreads=nthreads)
+    for w in walkers:
+        w.w.thermalization = 0
+    per_step = max(1, args.cpu_sweeps // 4)
+    for _ in range(args.warmup):
+        O.run_parallel(om, walkers, per_step, measure=True, nthreads=nthreads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        O.run_parallel(om, walkers, per_step, measure=True, nthreads=nthreads)
+    dt = time.perf_counter() - t0
+    value = len(walkers) * per_step * args.steps / dt
+    line = {
+        "impl": "reference",
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "i32+f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "walkers_per_step": len(walkers), "sweeps_per_step": per_step,
+                   "note": "CPU restatement of the reference sweep (Julia reference not runnable here)"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": nthreads, "kind": "port",
+                         "sample": f"{len(walkers)} chains x {per_step} sweeps per step after 300 thermalisation sweeps"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    rank, world, local = dist_setup(args)
+    S = _sse_loader.load()
+    from sse_gb300.engine import Engine
+
+    flat = S.flatten_model(make_model(S, args.side))
+    N = flat.nsites
+    eng = Engine(local)
+    mid = eng.register_model(flat)
+    nw = args.walkers
+    ids = eng.create_walkers(mid, [dict(T=1.0 / args.beta, seed=args.seed, stream=rank * nw + k,
+                                        thermalization=args.therm) for k in range(nw)])
+    eng.init(ids)
+    # thermalisation (controller active), in blocks
+    done = 0
+    while done < args.therm:
+        blk = min(100, args.therm - done)
+        eng.sweep(ids, blk, measure=True)
+        done += blk
+    launches_seen = 0
+    for _ in range(args.warmup):
+        eng.sweep(ids, args.sweeps_per_step, measure=True)
+        eng.observables(ids, reset=True)
+
+    info0 = [eng.info(int(i)) for i in ids]
+    clocks = ClockSampler(local)
+    barrier(world)
+    clocks.start()
+    step_ms = []
+    launches = 0
+    if args.profile:
+        eng.profiler_range(True)
+    for _ in range(args.steps):
+        eng.sweep(ids, args.sweeps_per_step, measure=True)
+        ms, nl = eng.last_timing()
+        step_ms.append(ms)
+        launches += nl
+    if args.profile:
+        eng.profiler_range(False)
+    clk = clocks.stop()
+    barrier(world)
+    info1 = [eng.info(int(i)) for i in ids]
+    dev_s = sum(step_ms) / 1e3
+    t_max = barrier_max(world, dev_s)
+    total_ws = barrier_sum(world, nw * args.sweeps_per_step * args.steps)
+    value = total_ws / t_max
+
+    slots = sum(b["slot_visits"] - a["slot_visits"] for a, b in zip(info0, info1))
+    worm = sum(b["worm_steps"] - a["worm_steps"] for a, b in zip(info0, info1))
+    opupd = barrier_sum(world, slots + worm) / t_max
+    # algorithmic bytes per launch of the sweep kernel (one launch per step)
+    nsw = args.sweeps_per_step * args.steps
+    bytes_total = sum(walker_bytes((b["slot_visits"] - a["slot_visits"]) / nsw, (b["worm_steps"] - a["worm_steps"]) / nsw, N) * nsw
+                      for a, b in zip(info0, info1))
+    per_launch_bytes = bytes_total / args.steps
+    avg_launch_s = dev_s / args.steps
+    achieved = per_launch_bytes / avg_launch_s / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = None
+    tfile = os.path.join(ROOT, "profiles", "k_walk_sweep_traffic.json")
+    if os.path.exists(tfile):
+        try:
+            with open(tfile) as f:
+                tj = json.load(f)
+            traffic = float(tj["dram_bytes_per_walker_sweep"]) * nw * args.sweeps_per_step
+        except Exception:
+            traffic = None
+
+    # end-to-end through the public API: ids H2D, sweep, observables D2H, wall clock
+    barrier(world)
+    t0 = time.perf_counter()
+    obs_bytes = 0
+    for _ in range(args.steps):
+        eng.sweep(ids, args.sweeps_per_step, measure=True)
+        out = eng.observables(ids, reset=True)
+        obs_bytes = sum(s.nbytes + c.nbytes + l.nbytes for s, c, l in out)
+    e2e_s = barrier_max(world, time.perf_counter() - t0)
+    e2e_value = total_ws / e2e_s
+
+    result = None
+    if rank == 0:
+        # plain path: one launch per walker per sweep (a per-walker sweep! call)
+        sub = ids[: args.plain_walkers]
+        eng.sweep(sub, 1, measure=True, plain=True)
+        t0 = time.perf_counter()
+        eng.sweep(sub, 2, measure=True, plain=True)
+        plain_s = time.perf_counter() - t0
+        plain_value = len(sub) * 2 / plain_s
+
+        states = [eng.export(int(i)) for i in ids[: (args.cpu_threads or os.cpu_count() or 1)]]
+        cpu = cpu_baseline(S, flat, states, args, args.cpu_threads or os.cpu_count() or 1)
+
+        mean_L = float(np.mean([x["L"] for x in info1]))
+        result = {
+            "metric": METRIC,
+            "value": value,
+            "unit": METRIC,
+            "n_gpus": world,
+            "steps": args.steps,
+            "warmup": args.warmup,
+            "ms_per_step": t_max * 1e3 / args.steps,
+            "higher_is_better": True,
+            "scaling": "weak",
+            "vs_baseline": None,
+            "dtype": "i32+f64",
+            "data": "synthetic",
+            "config": {
+                "workload": WORKLOAD,
+                "walkers": nw,
+                "side": args.side,
+                "beta": args.beta,
+                "thermalization_sweeps": args.therm,
+                "sweeps_per_step": args.sweeps_per_step,
+                "parallelism": f"replicas x{world}",
+                "l2": f"working set {sum(x['capacity'] for x in info1) * 40 / 1e9:.1f} GB of walker state, larger than L2",
+                "mean_cutoff_L": mean_L,
+            },
+            "operator_updates_per_s": opupd,
+            "plain": {"value": plain_value, "unit": METRIC, "walkers": len(sub),
+                      "path": "one kernel launch (one warp) per walker per sweep, synchronised after each"},
+            "batched_over_plain": value / plain_value,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "peak_kind": peak_kind, "kernel": "k_walk<SWEEP>",
+                         "algorithmic_bytes_per_launch": per_launch_bytes},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * len(ids),
+                    "d2h_bytes_per_step": obs_bytes},
+            "gpu_launches": launches,
+            "clocks": clk,
+        }
+        print(json.dumps(result), flush=True)
+    eng.close()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

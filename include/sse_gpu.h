@@ -1,0 +1,184 @@
+/*
+ * libssegpu -- C ABI of the GB300 SSE update engine.
+ *
+ * The engine runs the hot path of lukas-weber/StochasticSeriesExpansion.jl,
+ * one Carlo.jl MC step per walker:
+ *
+ *     Carlo.sweep!(mc, ctx)    src/sse.jl:62-68
+ *         diagonal_update      src/sse.jl:137-191
+ *         make_vertex_list!    src/vertex_list.jl:15-54
+ *         worm_update          src/sse.jl:193-303, scatter src/vertex_data.jl:106-125
+ *     Carlo.measure!(mc, ctx)  src/sse.jl:70-87, 305-376 (+ MagnetizationEstimator)
+ *
+ * for many independent walkers (Markov chains) on one GPU.  The library owns
+ * all device memory and one CUDA stream per engine; every call below is
+ * synchronous with respect to the host and returns an sse_status code.  No
+ * exception crosses the boundary; sse_engine_last_error() describes the last
+ * failure.  One host thread per engine.
+ *
+ * Random numbers: walker w with key `seed` and id `stream` draws its i-th
+ * 64-bit value from Philox4x32-10(counter = (i/2, stream), key = seed), words
+ * (0,1) for even i and (2,3) for odd i.  rand() = (u >> 11) * 2^-53 and
+ * rand(1:m) = 1 + floor(u*m / 2^64).  A walker's trajectory therefore depends
+ * only on its own (seed, stream) and inputs, never on the batch it runs in.
+ *
+ * Operator codes (uint32): 0 = identity; bit 0 = 1 otherwise, bit 1 =
+ * diagonal, bits 2..10 = vertex index (0-based), bits 11..31 = bond (0-based).
+ * Spin states are 0-based uint8 (the reference's StateIndex minus one).
+ */
+#ifndef SSE_GPU_H
+#define SSE_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SSE_GPU_ABI_VERSION 1
+
+typedef enum sse_status {
+  SSE_OK = 0,
+  SSE_ERR_ARG = 1,            /* bad argument (null pointer, unknown id, size out of range) */
+  SSE_ERR_CUDA = 2,           /* a CUDA runtime call failed */
+  SSE_ERR_CAPACITY = 3,       /* a walker needs more memory than allowed */
+  SSE_ERR_INVALID_VERTEX = 4, /* scatter found no outgoing step (src/vertex_data.jl:124) */
+  SSE_ERR_TIMEOUT = 5,        /* a bounded device wait gave up */
+  SSE_ERR_NOMEM = 6,          /* device or host allocation failed */
+  SSE_ERR_STATE = 7,          /* call not valid in the walker's current state */
+  SSE_ERR_WORM_CAP = 8,       /* a worm exceeded the step cap (64 * (L + 16)) */
+  SSE_ERR_UNSUPPORTED = 9     /* model outside the engine's limits */
+} sse_status;
+
+typedef struct sse_engine sse_engine;
+
+/*
+ * Flat model tables (the SSEData of src/sse_data.jl with its VertexData of
+ * src/vertex_data.jl:13-28, plus the magnetisation-estimator coefficients).
+ * Replaces the reference's `generate_sse_data(model)` output
+ * (src/abstract_model.jl:280, src/models/magnet/magnet.jl:169-184).
+ * All arrays are copied to the device by sse_model_register.
+ * Limits: two-site bonds only (leg count 4), < 2^21 bonds, <= 512 vertices
+ * per bond type, site dimension <= 255.
+ */
+typedef struct sse_model_desc {
+  int32_t nsites, nbonds, ntypes, maxdim, nest;
+  double energy_offset;   /* SSEData.energy_offset (sum over bonds) */
+  double norm_site_count; /* normalization_site_count(model) */
+  const int32_t *site_dims;      /* [nsites] */
+  const int32_t *bond_type;      /* [nbonds] 0-based type */
+  const int32_t *bond_sites;     /* [2*nbonds] 0-based sites */
+  const int32_t *type_dims;      /* [2*ntypes] */
+  const int32_t *type_nverts;    /* [ntypes] */
+  const int32_t *type_maxworm;   /* [ntypes] */
+  const int32_t *type_diag_off;  /* [ntypes] offset into diag_vertex */
+  const int32_t *type_vert_off;  /* [ntypes] offset into weight/sign and 4x leg_state */
+  const int32_t *type_trans_off; /* [ntypes] offset into trans_start/trans_count */
+  const int32_t *diag_vertex;    /* vertex code (diag | idx << 1) for compound state s0 + d0*s1, or -1 */
+  const double *weight;
+  const int8_t *sign;
+  const uint8_t *leg_state;      /* [vertex*4 + leg], 0-based states */
+  const int32_t *trans_start;    /* [(v*4 + leg)*maxworm + worm-1] first outcome, -1 invalid */
+  const int32_t *trans_count;    /* number of outcomes */
+  const double *out_cum;         /* cumulative probabilities */
+  const int32_t *out_target;     /* vertex code after the step */
+  const int8_t *out_leg;         /* outgoing leg, 0-based */
+  const int8_t *out_worm;        /* outgoing worm, 1-based */
+  const double *est_coef;        /* [(e*nsites + site)*maxdim + s] staggered sign * magnetization_state */
+} sse_model_desc;
+
+/* MC(params) + the SSE-level task parameters of docs/src/parameters.md (src/sse.jl:26-45) */
+typedef struct sse_walker_params {
+  double T;
+  uint64_t seed;
+  uint64_t stream;
+  int64_t init_opstring_cutoff;        /* < 0: round(nsites*T), ties to even */
+  int32_t diagonal_warmup_sweeps;      /* reference default 5 */
+  double init_num_worms;               /* reference default 5 */
+  double num_worms_attenuation_factor; /* reference default 0.01 */
+  double target_worm_length_fraction;  /* reference default 2.0 */
+  int64_t thermalization;              /* Carlo thermalization sweeps */
+} sse_walker_params;
+
+/* scalar walker state: the checkpoint fields of src/sse.jl:89-107 plus the replay counter */
+typedef struct sse_walker_info {
+  int64_t L;             /* opstring cutoff, length(mc.operators) */
+  int64_t num_operators; /* mc.num_operators */
+  int64_t capacity;      /* device slots reserved for the opstring */
+  int64_t sweeps;        /* Carlo ctx.sweeps */
+  uint64_t rng_counter;  /* draws consumed */
+  double num_worms;
+  double avg_worm_length;
+  double T;
+  int32_t status;        /* sse_status of the walker's last device work */
+  int32_t model;
+  int64_t resize_after_thermalization; /* count of "spin array resized after thermalization" */
+  int64_t slot_visits;   /* diagonal-update slot visits, cumulative */
+  int64_t worm_steps;    /* worm vertex visits (scatter calls), cumulative */
+  int64_t phase_cycles[4]; /* SM clock cycles in diagonal update, linking, worm update, measurement */
+} sse_walker_info;
+
+/* sse_sweep flags */
+#define SSE_SWEEP_MEASURE 1u /* Carlo.measure! after every sweep that leaves the walker thermalized */
+#define SSE_SWEEP_PLAIN 2u   /* one kernel launch per walker per sweep (the unbatched path) */
+#define SSE_SWEEP_GRAPH 4u   /* replay the sweep block from a captured CUDA graph */
+
+/* ---- engine ---- */
+int sse_engine_create(int32_t device, sse_engine **out);
+int sse_engine_destroy(sse_engine *eng);
+const char *sse_engine_last_error(const sse_engine *eng);
+int sse_abi_version(void);
+
+/* ---- models: replaces generate_sse_data / SSEData (src/sse_data.jl:34-42) ---- */
+int sse_model_register(sse_engine *eng, const sse_model_desc *desc, int32_t *model_id);
+/* number of observables per walker of a model: 6 + 5*nest (names in the same order as
+ * Sign, OperatorCount, SignOperatorCount, SignOperatorCount2, SignEnergy, WormLengthFraction,
+ * then per estimator SignMag, SignAbsMag, SignMag2, SignMag4, SignMagChi) */
+int sse_model_nobs(sse_engine *eng, int32_t model_id, int32_t *nobs);
+
+/* ---- walkers: replaces MC(params) (src/sse.jl:26-45) ---- */
+int sse_walkers_create(sse_engine *eng, int32_t model_id, int32_t count, const sse_walker_params *params,
+                       int32_t *ids);
+int sse_walkers_destroy(sse_engine *eng, int32_t count, const int32_t *ids);
+/* reserve opstring capacity up front so that no regrowth happens later */
+int sse_walkers_reserve(sse_engine *eng, int32_t count, const int32_t *ids, int64_t capacity);
+
+/* ---- Carlo.init! (src/sse.jl:47-60) ---- */
+int sse_walkers_init(sse_engine *eng, int32_t count, const int32_t *ids);
+
+/* ---- Carlo.sweep! + Carlo.measure! (src/sse.jl:62-87), nsweeps Carlo steps per walker:
+ *      is_thermalized = sweeps > thermalization; sweep!; sweeps += 1;
+ *      measure! if SSE_SWEEP_MEASURE and sweeps > thermalization ---- */
+int sse_sweep(sse_engine *eng, int32_t count, const int32_t *ids, int32_t nsweeps, uint32_t flags);
+
+/* observable sums/counts/last values, nobs per walker, walker-major; reset clears sums and counts */
+int sse_observables(sse_engine *eng, int32_t count, const int32_t *ids, double *sums, int64_t *counts, double *last,
+                    int32_t reset);
+
+/* ---- walker state: Carlo.write_checkpoint / read_checkpoint (src/sse.jl:89-107) ---- */
+int sse_walker_info_get(sse_engine *eng, int32_t id, sse_walker_info *info);
+/* ops: at least info.L entries; state: nsites entries */
+int sse_walker_export(sse_engine *eng, int32_t id, uint32_t *ops, int64_t ops_len, uint8_t *state,
+                      sse_walker_info *info);
+/* sets L, num_operators, sweeps, rng_counter, num_worms, avg_worm_length from info; capacity grows as needed */
+int sse_walker_import(sse_engine *eng, int32_t id, const uint32_t *ops, const uint8_t *state,
+                      const sse_walker_info *info);
+
+/* ---- the vertex list of a walker's current opstring, reference layout (src/vertex_list.jl:1-54):
+ *      vertices[4*p + leg] = 4*p' + leg' or -1 (L*4 entries), v_first/v_last per site ---- */
+int sse_vertex_list(sse_engine *eng, int32_t id, int32_t *vertices, int32_t *v_first, int32_t *v_last);
+
+/* ---- instrumentation ---- */
+/* device time (ms) of the kernels of the last sse_sweep / sse_walkers_init, and the number of kernel launches */
+int sse_last_timing(sse_engine *eng, double *ms, int64_t *launches);
+/* launch shape of the batched kernel: warps (walkers) per block; 0 = automatic */
+int sse_set_launch(sse_engine *eng, int32_t warps_per_block, int32_t blocks_per_sm);
+int sse_get_launch(sse_engine *eng, int32_t *warps_per_block, int32_t *blocks_per_sm);
+/* brackets a profiled region (cudaProfilerStart / cudaProfilerStop) for profilers started with
+ * collection off; start != 0 opens the region, 0 closes it */
+int sse_profiler_range(sse_engine *eng, int32_t start);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -17,3 +17,4 @@ from .magnet import (
     magnetization_estimator_standard_prefix,
 )
 from .tables import FlatModel, flatten_model, flatten_sse_data
+from . import engine

@@ -1,0 +1,1046 @@
+// libssegpu: kernels and the C-ABI host engine (see include/sse_gpu.h).
+//
+// Kernels
+//   k_walk<INIT>   Carlo.init! for a list of walkers (src/sse.jl:47-60)
+//   k_walk<SWEEP>  nsweeps Carlo steps per walker: sweep! + measure!
+//                  (src/sse.jl:62-87), persistent: each warp pulls walkers
+//                  from a work queue and runs all of their sweeps
+//   k_link_debug   vertex list of one walker (src/vertex_list.jl) for export
+//   k_gather_*     observable / status gathers for the host
+//
+// Device memory: one stream-ordered pool (cudaMallocAsync) per engine; each
+// walker owns its opstring, compact-record and slot-index arrays sized to a
+// capacity that grows (with a relaunch) when the reference's cutoff rule
+// (src/sse.jl:138-145) asks for more slots than reserved.
+#include <cuda_profiler_api.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "sse_device.cuh"
+#include "sse_gpu.h"
+
+using namespace sse;
+
+namespace {
+
+constexpr int MODE_INIT = 0;
+constexpr int MODE_SWEEP = 1;
+
+template <int MODE>
+__device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, uint32_t flags, long long add_sweeps,
+                               int *flag_counts, int lane) {
+  Chain c;
+  c.L = W->L;
+  c.n = W->n;
+  c.cap = W->cap;
+  c.ctr = W->ctr;
+  c.seed = W->seed;
+  c.stream = W->stream;
+  c.T = W->T;
+  WormCtl wc;
+  wc.num_worms = W->num_worms;
+  wc.avg_len = W->avg_len;
+  wc.att = W->att;
+  wc.target_frac = W->target_frac;
+  uint32_t *ops = W->ops;
+  uint8_t *state = W->state;
+  const int N = M.nsites;
+  long long sweeps = W->sweeps;
+  // first pass of an sse_sweep call sets the target; relaunches after a regrowth keep it
+  const long long target = add_sweeps >= 0 ? sweeps + add_sweeps : W->target;
+  const long long therm = W->therm;
+  long long resize_count = W->resize_after_therm;
+  long long slot_visits = W->slot_visits;
+  long long worm_steps = W->worm_steps;
+  long long need_L = 0;
+  int phase = W->phase;
+  int warmup_done = W->warmup_done;
+  int status = ST_OK;
+  uint8_t *sst = smem;
+  int32_t *vlast = reinterpret_cast<int32_t *>(smem);
+
+  if (MODE == MODE_INIT) {
+    if (phase == PH_NEW) {
+      // mc.state = [rand(1:dim) for sites] (src/sse.jl:48)
+      for (int i = lane; i < N; i += 32)
+        state[i] = (uint8_t)urange0(draw64(c.seed, c.stream, c.ctr + i), (unsigned long long)M.site_dims[i]);
+      c.ctr += N;
+      c.L = W->init_cutoff;
+      c.n = 0;
+      for (long long p = lane; p < c.L; p += 32) ops[p] = 0u;
+      phase = PH_WARMUP;
+      warmup_done = 0;
+      __syncwarp();
+    }
+    while (phase == PH_WARMUP && warmup_done < W->warmup) {
+      for (int i = lane; i < N; i += 32) sst[i] = state[i];
+      __syncwarp();
+      status = diag_update(M, c, ops, sst, false, resize_count, need_L, lane);
+      if (status != ST_OK) break;
+      slot_visits += c.L;
+      warmup_done++;
+    }
+    if (status == ST_OK && phase == PH_WARMUP) phase = PH_READY;
+  } else {
+    if (phase != PH_READY) {
+      status = ST_STATE;
+    } else {
+      long long cyc0 = 0, cyc1 = 0, cyc2 = 0, cyc3 = 0;
+      while (sweeps < target) {
+        const bool thermalized = sweeps > therm;
+        long long t0 = clock64();
+        for (int i = lane; i < N; i += 32) sst[i] = state[i];
+        __syncwarp();
+        status = diag_update(M, c, ops, sst, thermalized, resize_count, need_L, lane);
+        if (status != ST_OK) break;
+        slot_visits += c.L;
+        __syncwarp();
+        long long t1 = clock64();
+        build_links(M, c.L, ops, W->rec, W->cidx, W->vfirst, vlast, lane);
+        long long t2 = clock64();
+        double wlf = 0.0;
+        bool have_wlf = false;
+        status = worm_update(M, c, wc, ops, W->rec, W->cidx, W->vfirst, state,
+                             reinterpret_cast<unsigned long long *>(smem), thermalized, wlf, have_wlf, worm_steps,
+                             lane);
+        if (status != ST_OK) break;
+        if (have_wlf && lane == 0) observe(W, 5, wlf);
+        sweeps++;
+        long long t3 = clock64();
+        if ((flags & SSE_SWEEP_MEASURE) && sweeps > therm) measure(M, c, W, ops, state, lane);
+        __syncwarp();
+        long long t4 = clock64();
+        cyc0 += t1 - t0;
+        cyc1 += t2 - t1;
+        cyc2 += t3 - t2;
+        cyc3 += t4 - t3;
+      }
+      if (lane == 0) {
+        W->cyc[0] += cyc0;
+        W->cyc[1] += cyc1;
+        W->cyc[2] += cyc2;
+        W->cyc[3] += cyc3;
+      }
+    }
+  }
+  if (lane == 0) {
+    W->L = c.L;
+    W->n = c.n;
+    W->ctr = c.ctr;
+    W->num_worms = wc.num_worms;
+    W->avg_len = wc.avg_len;
+    W->sweeps = sweeps;
+    W->target = target;
+    W->resize_after_therm = resize_count;
+    W->slot_visits = slot_visits;
+    W->worm_steps = worm_steps;
+    W->phase = phase;
+    W->warmup_done = warmup_done;
+    W->status = status;
+    W->need_L = need_L;
+    if (status == ST_NEED_GROW) atomicAdd(flag_counts + 0, 1);
+    else if (status != ST_OK) atomicAdd(flag_counts + 1, 1);
+  }
+  __syncwarp();
+}
+
+// Persistent: every warp pulls walker indices from `queue` until `work` is exhausted.  With
+// single_id >= 0 the launch is one warp working on that walker only (the unbatched path).
+template <int MODE>
+__global__ void __launch_bounds__(128, 7) k_walk(const DevModel *__restrict__ models, DevWalker *__restrict__ walkers,
+                                              const int32_t *__restrict__ work, int nwork, int single_id, int *queue,
+                                              uint32_t flags, long long add_sweeps, int smem_per_warp,
+                                              int *flag_counts) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int lane = threadIdx.x & 31;
+  uint8_t *mine = smem + (size_t)(threadIdx.x >> 5) * smem_per_warp;
+  if (single_id >= 0) {
+    DevWalker *W = walkers + single_id;
+    process_walker<MODE>(models[W->model], W, mine, flags, add_sweeps, flag_counts, lane);
+    return;
+  }
+  for (;;) {
+    int idx = 0;
+    if (lane == 0) idx = atomicAdd(queue, 1);
+    idx = __shfl_sync(FULL, idx, 0);
+    if (idx >= nwork) break;
+    DevWalker *W = walkers + work[idx];
+    process_walker<MODE>(models[W->model], W, mine, flags, add_sweeps, flag_counts, lane);
+  }
+}
+
+__global__ void k_link_debug(const DevModel *models, DevWalker *walkers, int id, int32_t *vlast_out) {
+  extern __shared__ __align__(16) uint8_t smem[];
+  const int lane = threadIdx.x & 31;
+  DevWalker *W = walkers + id;
+  const DevModel &M = models[W->model];
+  int32_t *vlast = reinterpret_cast<int32_t *>(smem);
+  build_links(M, W->L, W->ops, W->rec, W->cidx, W->vfirst, vlast, lane);
+  for (int i = lane; i < M.nsites; i += 32) vlast_out[i] = vlast[i];
+}
+
+__global__ void k_gather_status(const DevWalker *walkers, const int32_t *ids, int n, int32_t *status,
+                                long long *need_L) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    status[i] = walkers[ids[i]].status;
+    need_L[i] = walkers[ids[i]].need_L;
+  }
+}
+
+__global__ void k_gather_obs(DevWalker *walkers, const int32_t *ids, int n, const int32_t *offsets, double *sums,
+                             long long *counts, double *last, int reset) {
+  const int w = blockIdx.x;
+  if (w >= n) return;
+  DevWalker *W = walkers + ids[w];
+  const int off = offsets[w], cnt = offsets[w + 1] - offsets[w];
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) {
+    sums[off + i] = W->obs_sum[i];
+    counts[off + i] = W->obs_count[i];
+    last[off + i] = W->obs_last[i];
+    if (reset) {
+      W->obs_sum[i] = 0.0;
+      W->obs_count[i] = 0;
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host engine
+// ---------------------------------------------------------------------------
+
+struct HostModel {
+  DevModel dev{};
+  std::vector<void *> allocs;
+  int32_t nsites = 0, nobs = 0;
+};
+
+struct HostWalker {
+  bool alive = false;
+  int32_t model = -1;
+  long long cap = 0;
+  uint32_t *ops = nullptr;
+  Rec *rec = nullptr;
+  int32_t *cidx = nullptr;
+  int32_t *vfirst = nullptr;
+  uint8_t *state = nullptr;
+  double *obs_sum = nullptr, *obs_last = nullptr;
+  long long *obs_count = nullptr;
+};
+
+struct sse_engine {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int num_sms = 0;
+  std::vector<HostModel> models;
+  DevModel *d_models = nullptr;
+  size_t d_models_cap = 0;
+  std::vector<HostWalker> walkers;
+  DevWalker *d_walkers = nullptr;
+  size_t d_walkers_cap = 0;
+  int32_t *d_work = nullptr;
+  size_t work_cap = 0;
+  int *d_queue = nullptr;      // [0] queue head
+  int *d_flags = nullptr;      // [0] need-grow count, [1] error count
+  int32_t *d_status = nullptr; // gather buffers
+  long long *d_needL = nullptr;
+  size_t status_cap = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  double last_ms = 0.0;
+  long long last_launches = 0;
+  int warps_per_block = 0, blocks_per_sm = 0;
+  std::map<std::pair<std::vector<int32_t>, long long>, cudaGraphExec_t> graphs;
+};
+
+namespace {
+
+int fail(sse_engine *e, int code, const std::string &msg) {
+  if (e) e->err = msg;
+  return code;
+}
+
+#define CUDA_TRY(e, call)                                                                          \
+  do {                                                                                             \
+    cudaError_t _st = (call);                                                                      \
+    if (_st != cudaSuccess)                                                                        \
+      return fail((e), SSE_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_st));         \
+  } while (0)
+
+template <class T>
+int dev_alloc(sse_engine *e, T **p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  cudaError_t st = cudaMallocAsync((void **)p, count * sizeof(T), e->stream);
+  if (st != cudaSuccess) return fail(e, SSE_ERR_NOMEM, std::string("cudaMallocAsync: ") + cudaGetErrorString(st));
+  return SSE_OK;
+}
+
+template <class T>
+void dev_free(sse_engine *e, T *&p) {
+  if (p) cudaFreeAsync(p, e->stream);
+  p = nullptr;
+}
+
+template <class T>
+int upload(sse_engine *e, HostModel &hm, const T *src, size_t count, const T **dst) {
+  T *d = nullptr;
+  int rc = dev_alloc(e, &d, count);
+  if (rc) return rc;
+  hm.allocs.push_back(d);
+  if (count && src) CUDA_TRY(e, cudaMemcpyAsync(d, src, count * sizeof(T), cudaMemcpyHostToDevice, e->stream));
+  *dst = d;
+  return SSE_OK;
+}
+
+bool valid_id(sse_engine *e, int32_t id) {
+  return id >= 0 && (size_t)id < e->walkers.size() && e->walkers[id].alive;
+}
+
+int ensure_work(sse_engine *e, size_t n) {
+  if (n <= e->work_cap) return SSE_OK;
+  size_t cap = std::max<size_t>(n, 2 * e->work_cap);
+  dev_free(e, e->d_work);
+  dev_free(e, e->d_status);
+  dev_free(e, e->d_needL);
+  int rc = dev_alloc(e, &e->d_work, cap);
+  if (!rc) rc = dev_alloc(e, &e->d_status, cap);
+  if (!rc) rc = dev_alloc(e, &e->d_needL, cap);
+  if (rc) return rc;
+  e->work_cap = cap;
+  e->status_cap = cap;
+  return SSE_OK;
+}
+
+int read_walker(sse_engine *e, int32_t id, DevWalker &w) {
+  CUDA_TRY(e, cudaMemcpyAsync(&w, e->d_walkers + id, sizeof(DevWalker), cudaMemcpyDeviceToHost, e->stream));
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  return SSE_OK;
+}
+
+int write_walker(sse_engine *e, int32_t id, const DevWalker &w) {
+  CUDA_TRY(e, cudaMemcpyAsync(e->d_walkers + id, &w, sizeof(DevWalker), cudaMemcpyHostToDevice, e->stream));
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  return SSE_OK;
+}
+
+// Grow walker `id` so that at least `need` slots fit; the opstring prefix [0, L) is preserved.
+int grow_walker(sse_engine *e, int32_t id, long long need) {
+  DevWalker w;
+  int rc = read_walker(e, id, w);
+  if (rc) return rc;
+  HostWalker &h = e->walkers[id];
+  if (need <= h.cap) return SSE_OK;
+  long long cap = std::max<long long>(need, 2 * h.cap);
+  cap = (cap + 63) & ~63LL;
+  if (cap >= (1LL << 31) / 4) return fail(e, SSE_ERR_CAPACITY, "walker opstring exceeds 2^29 slots");
+  uint32_t *ops = nullptr;
+  Rec *rec = nullptr;
+  int32_t *cidx = nullptr;
+  rc = dev_alloc(e, &ops, (size_t)cap);
+  if (!rc) rc = dev_alloc(e, &rec, (size_t)cap);
+  if (!rc) rc = dev_alloc(e, &cidx, (size_t)cap);
+  if (rc) return rc;
+  if (h.ops && w.L > 0)
+    CUDA_TRY(e, cudaMemcpyAsync(ops, h.ops, sizeof(uint32_t) * (size_t)w.L, cudaMemcpyDeviceToDevice, e->stream));
+  dev_free(e, h.ops);
+  dev_free(e, h.rec);
+  dev_free(e, h.cidx);
+  h.ops = ops;
+  h.rec = rec;
+  h.cidx = cidx;
+  h.cap = cap;
+  w.ops = ops;
+  w.rec = rec;
+  w.cidx = cidx;
+  w.cap = cap;
+  if (w.status == ST_NEED_GROW) w.status = ST_OK;
+  w.need_L = 0;
+  return write_walker(e, id, w);
+}
+
+int choose_launch(sse_engine *e, int max_nsites, int nwork, int &wpb, int &grid, int &smem_per_warp, bool init) {
+  // per warp: spin state (N bytes, diagonal update), per-site link tails (4N, linking), 64 draws (512 B, worms)
+  smem_per_warp = ((std::max(4 * std::max(max_nsites, 1), 512)) + 15) & ~15;
+  wpb = e->warps_per_block > 0 ? e->warps_per_block : 4;
+  if (wpb > 4) wpb = 4;  // k_walk is compiled for at most 128 threads per block
+  while (wpb > 1 && (size_t)wpb * smem_per_warp > 200 * 1024) wpb >>= 1;
+  const size_t smem = (size_t)wpb * smem_per_warp;
+  if (smem > 227 * 1024) return fail(e, SSE_ERR_UNSUPPORTED, "per-walker shared memory exceeds the SM limit");
+  const void *fn = init ? (const void *)k_walk<MODE_INIT> : (const void *)k_walk<MODE_SWEEP>;
+  CUDA_TRY(e, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::max<size_t>(smem, 48 * 1024)));
+  int per_sm = 0;
+  CUDA_TRY(e, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, 32 * wpb, smem));
+  if (per_sm < 1) return fail(e, SSE_ERR_UNSUPPORTED, "kernel does not fit on an SM with this launch shape");
+  if (e->blocks_per_sm > 0) per_sm = std::min(per_sm, e->blocks_per_sm);
+  const long long resident = (long long)per_sm * e->num_sms;
+  const long long needed = (nwork + wpb - 1) / wpb;
+  grid = (int)std::max<long long>(1, std::min(resident, needed));
+  return SSE_OK;
+}
+
+// Launch one pass: persistent over d_work[0..nwork) when single_id < 0, else one warp on single_id.
+int launch_pass(sse_engine *e, int mode, int nwork, int single_id, uint32_t flags, long long add_sweeps,
+                int max_nsites) {
+  int wpb, grid, spw;
+  int rc = choose_launch(e, max_nsites, nwork, wpb, grid, spw, mode == MODE_INIT);
+  if (rc) return rc;
+  if (single_id >= 0) {
+    grid = 1;
+    wpb = 1;
+  } else {
+    CUDA_TRY(e, cudaMemsetAsync(e->d_queue, 0, sizeof(int), e->stream));
+  }
+  if (mode == MODE_INIT)
+    k_walk<MODE_INIT><<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(
+        e->d_models, e->d_walkers, e->d_work, nwork, single_id, e->d_queue, flags, add_sweeps, spw, e->d_flags);
+  else
+    k_walk<MODE_SWEEP><<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(
+        e->d_models, e->d_walkers, e->d_work, nwork, single_id, e->d_queue, flags, add_sweeps, spw, e->d_flags);
+  CUDA_TRY(e, cudaGetLastError());
+  e->last_launches += 1;
+  return SSE_OK;
+}
+
+int max_nsites_of(sse_engine *e, int n, const int32_t *ids) {
+  int m = 1;
+  for (int i = 0; i < n; i++) m = std::max(m, e->models[e->walkers[ids[i]].model].nsites);
+  return m;
+}
+
+// Runs `mode` over the given walkers until none of them needs to grow.  With SSE_SWEEP_PLAIN and a
+// single walker the pass is one warp launched for that walker alone.
+int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long nsweeps, uint32_t flags) {
+  float ms_total = 0.0f;
+  e->last_launches = 0;
+  bool first = true;
+  const bool single = (flags & SSE_SWEEP_PLAIN) && work.size() == 1;
+  for (int round = 0; round < 64 && !work.empty(); round++) {
+    const int n = (int)work.size();
+    const int max_ns = max_nsites_of(e, n, work.data());
+    int rc = SSE_OK;
+    if (!single) {
+      // longest walkers first: they bound the makespan of the persistent pass
+      std::stable_sort(work.begin(), work.end(),
+                       [&](int32_t a, int32_t b) { return e->walkers[a].cap > e->walkers[b].cap; });
+      rc = ensure_work(e, work.size());
+      if (rc) return rc;
+      CUDA_TRY(e, cudaMemcpyAsync(e->d_work, work.data(), sizeof(int32_t) * work.size(), cudaMemcpyHostToDevice,
+                                  e->stream));
+    }
+    CUDA_TRY(e, cudaMemsetAsync(e->d_flags, 0, 2 * sizeof(int), e->stream));
+    CUDA_TRY(e, cudaEventRecord(e->ev0, e->stream));
+    rc = launch_pass(e, mode, n, single ? work[0] : -1, flags, (mode == MODE_SWEEP && first) ? nsweeps : -1, max_ns);
+    if (rc) return rc;
+    first = false;
+    CUDA_TRY(e, cudaEventRecord(e->ev1, e->stream));
+    int flags_h[2];
+    CUDA_TRY(e, cudaMemcpyAsync(flags_h, e->d_flags, sizeof(flags_h), cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+    float ms = 0.0f;
+    CUDA_TRY(e, cudaEventElapsedTime(&ms, e->ev0, e->ev1));
+    ms_total += ms;
+    if (flags_h[0] == 0 && flags_h[1] == 0) break;
+    // some walker stopped: collect statuses
+    if (single) {
+      rc = ensure_work(e, 1);
+      if (rc) return rc;
+      CUDA_TRY(e, cudaMemcpyAsync(e->d_work, work.data(), sizeof(int32_t), cudaMemcpyHostToDevice, e->stream));
+    }
+    k_gather_status<<<(n + 255) / 256, 256, 0, e->stream>>>(e->d_walkers, e->d_work, n, e->d_status, e->d_needL);
+    CUDA_TRY(e, cudaGetLastError());
+    std::vector<int32_t> st(n);
+    std::vector<long long> needL(n);
+    CUDA_TRY(e, cudaMemcpyAsync(st.data(), e->d_status, sizeof(int32_t) * n, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(e, cudaMemcpyAsync(needL.data(), e->d_needL, sizeof(long long) * n, cudaMemcpyDeviceToHost, e->stream));
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+    std::vector<int32_t> again;
+    for (int i = 0; i < n; i++) {
+      if (st[i] == ST_NEED_GROW) {
+        rc = grow_walker(e, work[i], needL[i]);
+        if (rc) return rc;
+        again.push_back(work[i]);
+      } else if (st[i] != ST_OK) {
+        char buf[128];
+        snprintf(buf, sizeof buf, "walker %d stopped with status %d", work[i], st[i]);
+        return fail(e, st[i], buf);
+      }
+    }
+    work.swap(again);
+  }
+  if (!work.empty() && e->last_launches >= 64) return fail(e, SSE_ERR_CAPACITY, "walkers kept needing regrowth");
+  e->last_ms = ms_total;
+  return SSE_OK;
+}
+
+int upload_models(sse_engine *e) {
+  if (e->models.size() > e->d_models_cap) {
+    dev_free(e, e->d_models);
+    size_t cap = std::max<size_t>(8, 2 * e->models.size());
+    int rc = dev_alloc(e, &e->d_models, cap);
+    if (rc) return rc;
+    e->d_models_cap = cap;
+  }
+  std::vector<DevModel> h(e->models.size());
+  for (size_t i = 0; i < e->models.size(); i++) h[i] = e->models[i].dev;
+  CUDA_TRY(e, cudaMemcpyAsync(e->d_models, h.data(), sizeof(DevModel) * h.size(), cudaMemcpyHostToDevice, e->stream));
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  return SSE_OK;
+}
+
+int ensure_walker_slots(sse_engine *e, size_t n) {
+  if (n <= e->d_walkers_cap) return SSE_OK;
+  size_t cap = std::max<size_t>(n, std::max<size_t>(64, 2 * e->d_walkers_cap));
+  DevWalker *nw = nullptr;
+  int rc = dev_alloc(e, &nw, cap);
+  if (rc) return rc;
+  CUDA_TRY(e, cudaMemsetAsync(nw, 0, sizeof(DevWalker) * cap, e->stream));
+  if (e->d_walkers)
+    CUDA_TRY(e, cudaMemcpyAsync(nw, e->d_walkers, sizeof(DevWalker) * e->d_walkers_cap, cudaMemcpyDeviceToDevice,
+                                e->stream));
+  dev_free(e, e->d_walkers);
+  e->d_walkers = nw;
+  e->d_walkers_cap = cap;
+  for (auto &g : e->graphs) cudaGraphExecDestroy(g.second);
+  e->graphs.clear();
+  return SSE_OK;
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+extern "C" {
+
+int sse_abi_version(void) { return SSE_GPU_ABI_VERSION; }
+
+int sse_engine_create(int32_t device, sse_engine **out) {
+  if (!out) return SSE_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return SSE_ERR_CUDA;
+  sse_engine *e = new sse_engine();
+  e->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete e;
+    return SSE_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {
+    delete e;
+    return SSE_ERR_CUDA;
+  }
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+    unsigned long long thr = ~0ull;  // keep freed blocks cached in the pool
+    cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+  }
+  if (dev_alloc(e, &e->d_queue, 4) || dev_alloc(e, &e->d_flags, 4)) {
+    sse_engine_destroy(e);
+    return SSE_ERR_NOMEM;
+  }
+  *out = e;
+  return SSE_OK;
+}
+
+int sse_engine_destroy(sse_engine *e) {
+  if (!e) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  for (auto &g : e->graphs) cudaGraphExecDestroy(g.second);
+  for (auto &w : e->walkers) {
+    dev_free(e, w.ops);
+    dev_free(e, w.rec);
+    dev_free(e, w.cidx);
+    dev_free(e, w.vfirst);
+    dev_free(e, w.state);
+    dev_free(e, w.obs_sum);
+    dev_free(e, w.obs_last);
+    dev_free(e, w.obs_count);
+  }
+  for (auto &m : e->models)
+    for (void *p : m.allocs) cudaFreeAsync(p, e->stream);
+  dev_free(e, e->d_models);
+  dev_free(e, e->d_walkers);
+  dev_free(e, e->d_work);
+  dev_free(e, e->d_status);
+  dev_free(e, e->d_needL);
+  dev_free(e, e->d_queue);
+  dev_free(e, e->d_flags);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->ev0) cudaEventDestroy(e->ev0);
+  if (e->ev1) cudaEventDestroy(e->ev1);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+  return SSE_OK;
+}
+
+const char *sse_engine_last_error(const sse_engine *e) { return e ? e->err.c_str() : "null engine"; }
+
+int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id) {
+  if (!e || !d || !model_id) return SSE_ERR_ARG;
+  if (d->nsites <= 0 || d->nbonds <= 0 || d->ntypes <= 0 || d->nest < 0)
+    return fail(e, SSE_ERR_ARG, "model sizes must be positive");
+  if (d->nbonds >= (1 << 21)) return fail(e, SSE_ERR_UNSUPPORTED, "at most 2^21 - 1 bonds");
+  if (d->maxdim < 2 || d->maxdim > 255) return fail(e, SSE_ERR_UNSUPPORTED, "site dimension must be 2..255");
+  cudaSetDevice(e->device);
+  HostModel hm;
+  hm.nsites = d->nsites;
+  hm.nobs = 6 + 5 * d->nest;
+  DevModel &m = hm.dev;
+  m.nsites = d->nsites;
+  m.nbonds = d->nbonds;
+  m.ntypes = d->ntypes;
+  m.maxdim = d->maxdim;
+  m.nest = d->nest;
+  m.nobs = hm.nobs;
+  m.energy_offset = d->energy_offset;
+  m.norm_site_count = d->norm_site_count;
+  // validate and pack bonds
+  std::vector<int4> bi(d->nbonds);
+  for (int b = 0; b < d->nbonds; b++) {
+    const int s0 = d->bond_sites[2 * b], s1 = d->bond_sites[2 * b + 1], t = d->bond_type[b];
+    if (s0 < 0 || s1 < 0 || s0 >= d->nsites || s1 >= d->nsites || s0 == s1 || t < 0 || t >= d->ntypes)
+      return fail(e, SSE_ERR_ARG, "bond " + std::to_string(b) + " has invalid sites or type");
+    bi[b] = make_int4(s0, s1, t, 0);
+  }
+  size_t ndiag = 0, nvert = 0, ntrans = 0, nout = 0;
+  std::vector<DevType> types(d->ntypes);
+  for (int t = 0; t < d->ntypes; t++) {
+    DevType &x = types[t];
+    x.d0 = d->type_dims[2 * t];
+    x.d1 = d->type_dims[2 * t + 1];
+    x.nverts = d->type_nverts[t];
+    x.maxworm = d->type_maxworm[t];
+    x.diag_off = d->type_diag_off[t];
+    x.vert_off = d->type_vert_off[t];
+    x.trans_off = d->type_trans_off[t];
+    x.pad = 0;
+    if (x.nverts <= 0 || x.nverts > 512) return fail(e, SSE_ERR_UNSUPPORTED, "vertex count per type must be 1..512");
+    if (x.d0 < 2 || x.d1 < 2 || x.maxworm < 1) return fail(e, SSE_ERR_ARG, "bad type dims");
+    ndiag = std::max(ndiag, (size_t)x.diag_off + (size_t)x.d0 * x.d1);
+    nvert = std::max(nvert, (size_t)x.vert_off + x.nverts);
+    ntrans = std::max(ntrans, (size_t)x.trans_off + (size_t)x.nverts * 4 * x.maxworm);
+  }
+  for (size_t i = 0; i < ntrans; i++) {
+    if (d->trans_start[i] >= 0) nout = std::max(nout, (size_t)d->trans_start[i] + (size_t)d->trans_count[i]);
+  }
+  for (int b = 0; b < d->nbonds; b++) {
+    const DevType &x = types[bi[b].z];
+    if (d->site_dims[bi[b].x] != x.d0 || d->site_dims[bi[b].y] != x.d1)
+      return fail(e, SSE_ERR_ARG, "site dimensions inconsistent with bond type dims");
+  }
+  int rc = upload(e, hm, bi.data(), bi.size(), &m.bond_info);
+  if (!rc) rc = upload(e, hm, d->site_dims, (size_t)d->nsites, &m.site_dims);
+  if (!rc) rc = upload(e, hm, types.data(), types.size(), &m.types);
+  if (!rc) rc = upload(e, hm, d->diag_vertex, ndiag, &m.diag_vertex);
+  // weight classes: the distinct weights of diagonal vertices; the diagonal update compares
+  // random integers against per-class thresholds
+  std::vector<double> cls_w;
+  std::vector<int8_t> vclass(nvert, (int8_t)-1);
+  for (int t = 0; t < d->ntypes; t++) {
+    for (int v = 0; v < types[t].nverts; v++) {
+      const size_t vo = (size_t)types[t].vert_off + v;
+      const uint8_t *ls = d->leg_state + 4 * vo;
+      if (ls[0] != ls[2] || ls[1] != ls[3]) continue;
+      const double w = d->weight[vo];
+      size_t c = 0;
+      while (c < cls_w.size() && cls_w[c] != w) c++;
+      if (c == cls_w.size()) cls_w.push_back(w);
+      vclass[vo] = (int8_t)std::min<size_t>(c, 127);
+    }
+  }
+  std::vector<int32_t> diag_vc(ndiag, -1);
+  for (int t = 0; t < d->ntypes; t++) {
+    const int nst = types[t].d0 * types[t].d1;
+    for (int st = 0; st < nst; st++) {
+      const size_t i = (size_t)types[t].diag_off + st;
+      const int vc = d->diag_vertex[i];
+      if (vc < 0) continue;
+      if ((vc >> 1) >= types[t].nverts || !(vc & 1)) return fail(e, SSE_ERR_ARG, "bad diagonal vertex table");
+      const int cls = vclass[(size_t)types[t].vert_off + (vc >> 1)];
+      if (cls < 0) return fail(e, SSE_ERR_ARG, "diagonal vertex table points at an off-diagonal vertex");
+      diag_vc[i] = vc | (cls << 16);
+    }
+  }
+  m.ncls = (int32_t)cls_w.size();
+  if (cls_w.empty()) cls_w.push_back(0.0);
+  if (!rc) rc = upload(e, hm, diag_vc.data(), ndiag, &m.diag_vc);
+  if (!rc) rc = upload(e, hm, vclass.data(), nvert, &m.vclass);
+  if (!rc) rc = upload(e, hm, cls_w.data(), cls_w.size(), &m.cls_w);
+  if (!rc) rc = upload(e, hm, d->weight, nvert, &m.weight);
+  if (!rc) rc = upload(e, hm, d->sign, nvert, &m.sign);
+  if (!rc) rc = upload(e, hm, d->leg_state, 4 * nvert, &m.leg_state);
+  // scatter tables with integer thresholds: u53 < ceil(cum * 2^53)  <=>  u53 * 2^-53 < cum
+  auto threshold = [](double cum) -> unsigned long long {
+    if (!(cum > 0.0)) return 0ull;
+    if (cum >= 1.0) return 1ull << 53;
+    return (unsigned long long)std::ceil(std::ldexp(cum, 53));
+  };
+  std::vector<Outcome> outc(nout);
+  for (size_t o = 0; o < nout; o++) {
+    const int leg = d->out_leg[o], worm = d->out_worm[o], tgt = d->out_target[o];
+    if (leg < 0 || leg > 3 || worm < 1 || worm > 255 || tgt < 0 || tgt >= 1024)
+      return fail(e, SSE_ERR_ARG, "transition outcome out of range");
+    outc[o].thr = threshold(d->out_cum[o]);
+    outc[o].packed = leg | (worm << 2) | (tgt << 10);
+    outc[o].pad = 0;
+  }
+  std::vector<Trans> trans(ntrans);
+  for (size_t i = 0; i < ntrans; i++) {
+    const int start = d->trans_start[i], cnt = d->trans_count[i];
+    if (start < 0 || cnt <= 0) {
+      trans[i].thr0 = 0;
+      trans[i].packed0 = -1;
+      trans[i].rest = 0;
+      continue;
+    }
+    if (cnt > 256 || start + 1 >= (1 << 23)) return fail(e, SSE_ERR_UNSUPPORTED, "transition row too long");
+    trans[i].thr0 = outc[start].thr;
+    trans[i].packed0 = outc[start].packed;
+    trans[i].rest = ((start + 1) << 8) | (cnt - 1);
+  }
+  if (!rc) rc = upload(e, hm, trans.data(), ntrans, &m.trans);
+  if (!rc) rc = upload(e, hm, outc.data(), nout, &m.outc);
+  if (!rc) rc = upload(e, hm, d->est_coef, (size_t)d->nest * d->nsites * d->maxdim, &m.est_coef);
+  if (rc) {
+    for (void *p : hm.allocs) cudaFreeAsync(p, e->stream);
+    return rc;
+  }
+  e->models.push_back(hm);
+  rc = upload_models(e);
+  if (rc) return rc;
+  *model_id = (int32_t)e->models.size() - 1;
+  return SSE_OK;
+}
+
+int sse_model_nobs(sse_engine *e, int32_t model_id, int32_t *nobs) {
+  if (!e || !nobs || model_id < 0 || (size_t)model_id >= e->models.size()) return SSE_ERR_ARG;
+  *nobs = e->models[model_id].nobs;
+  return SSE_OK;
+}
+
+int sse_walkers_create(sse_engine *e, int32_t model_id, int32_t count, const sse_walker_params *params,
+                       int32_t *ids) {
+  if (!e || !params || !ids || count < 0 || model_id < 0 || (size_t)model_id >= e->models.size())
+    return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  const HostModel &hm = e->models[model_id];
+  const size_t first = e->walkers.size();
+  int rc = ensure_walker_slots(e, first + count);
+  if (rc) return rc;
+  std::vector<DevWalker> dw(count);
+  for (int i = 0; i < count; i++) {
+    const sse_walker_params &p = params[i];
+    if (!(p.T > 0) || p.diagonal_warmup_sweeps < 0 || !(p.init_num_worms >= 0))
+      return fail(e, SSE_ERR_ARG, "walker parameters out of range");
+    HostWalker h;
+    h.alive = true;
+    h.model = model_id;
+    long long cutoff = p.init_opstring_cutoff;
+    if (cutoff < 0) cutoff = (long long)std::nearbyint((double)hm.nsites * p.T);  // round(Int, N*T), ties to even
+    h.cap = std::max<long long>(256, ((2 * cutoff + 100) + 63) & ~63LL);
+    rc = dev_alloc(e, &h.ops, (size_t)h.cap);
+    if (!rc) rc = dev_alloc(e, &h.rec, (size_t)h.cap);
+    if (!rc) rc = dev_alloc(e, &h.cidx, (size_t)h.cap);
+    if (!rc) rc = dev_alloc(e, &h.vfirst, (size_t)hm.nsites);
+    if (!rc) rc = dev_alloc(e, &h.state, (size_t)hm.nsites);
+    if (!rc) rc = dev_alloc(e, &h.obs_sum, (size_t)hm.nobs);
+    if (!rc) rc = dev_alloc(e, &h.obs_last, (size_t)hm.nobs);
+    if (!rc) rc = dev_alloc(e, &h.obs_count, (size_t)hm.nobs);
+    if (rc) return rc;
+    CUDA_TRY(e, cudaMemsetAsync(h.obs_sum, 0, sizeof(double) * hm.nobs, e->stream));
+    CUDA_TRY(e, cudaMemsetAsync(h.obs_last, 0, sizeof(double) * hm.nobs, e->stream));
+    CUDA_TRY(e, cudaMemsetAsync(h.obs_count, 0, sizeof(long long) * hm.nobs, e->stream));
+    CUDA_TRY(e, cudaMemsetAsync(h.state, 0, (size_t)hm.nsites, e->stream));
+    DevWalker &w = dw[i];
+    memset(&w, 0, sizeof w);
+    w.ops = h.ops;
+    w.rec = h.rec;
+    w.cidx = h.cidx;
+    w.vfirst = h.vfirst;
+    w.state = h.state;
+    w.obs_sum = h.obs_sum;
+    w.obs_last = h.obs_last;
+    w.obs_count = h.obs_count;
+    w.cap = h.cap;
+    w.T = p.T;
+    w.num_worms = p.init_num_worms;
+    w.avg_len = 1.0;
+    w.att = p.num_worms_attenuation_factor;
+    w.target_frac = p.target_worm_length_fraction;
+    w.seed = p.seed;
+    w.stream = p.stream;
+    w.therm = p.thermalization;
+    w.init_cutoff = cutoff;
+    w.model = model_id;
+    w.phase = PH_NEW;
+    w.warmup = p.diagonal_warmup_sweeps;
+    e->walkers.push_back(h);
+    ids[i] = (int32_t)(first + i);
+  }
+  if (count)
+    CUDA_TRY(e, cudaMemcpyAsync(e->d_walkers + first, dw.data(), sizeof(DevWalker) * count, cudaMemcpyHostToDevice,
+                                e->stream));
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  return SSE_OK;
+}
+
+int sse_walkers_destroy(sse_engine *e, int32_t count, const int32_t *ids) {
+  if (!e || (count && !ids)) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  for (int i = 0; i < count; i++) {
+    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+    HostWalker &h = e->walkers[ids[i]];
+    dev_free(e, h.ops);
+    dev_free(e, h.rec);
+    dev_free(e, h.cidx);
+    dev_free(e, h.vfirst);
+    dev_free(e, h.state);
+    dev_free(e, h.obs_sum);
+    dev_free(e, h.obs_last);
+    dev_free(e, h.obs_count);
+    h.alive = false;
+  }
+  for (auto &g : e->graphs) cudaGraphExecDestroy(g.second);
+  e->graphs.clear();
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  return SSE_OK;
+}
+
+int sse_walkers_reserve(sse_engine *e, int32_t count, const int32_t *ids, int64_t capacity) {
+  if (!e || (count && !ids) || capacity < 0) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  for (int i = 0; i < count; i++) {
+    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+    int rc = grow_walker(e, ids[i], capacity);
+    if (rc) return rc;
+  }
+  return SSE_OK;
+}
+
+int sse_walkers_init(sse_engine *e, int32_t count, const int32_t *ids) {
+  if (!e || (count && !ids)) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  std::vector<int32_t> work(ids, ids + count);
+  for (int32_t id : work)
+    if (!valid_id(e, id)) return fail(e, SSE_ERR_ARG, "unknown walker id");
+  return run_until_done(e, MODE_INIT, work, 0, 0);
+}
+
+int sse_sweep(sse_engine *e, int32_t count, const int32_t *ids, int32_t nsweeps, uint32_t flags) {
+  if (!e || (count && !ids) || nsweeps < 0) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  std::vector<int32_t> work(ids, ids + count);
+  for (int32_t id : work)
+    if (!valid_id(e, id)) return fail(e, SSE_ERR_ARG, "unknown walker id");
+  if (flags & SSE_SWEEP_PLAIN) {
+    // one launch per walker per sweep
+    double ms = 0.0;
+    long long launches = 0;
+    for (int32_t id : work) {
+      for (int s = 0; s < nsweeps; s++) {
+        int rc = run_until_done(e, MODE_SWEEP, std::vector<int32_t>{id}, 1, flags);
+        if (rc) return rc;
+        ms += e->last_ms;
+        launches += e->last_launches;
+      }
+    }
+    e->last_ms = ms;
+    e->last_launches = launches;
+    return SSE_OK;
+  }
+  return run_until_done(e, MODE_SWEEP, work, nsweeps, flags);
+}
+
+int sse_observables(sse_engine *e, int32_t count, const int32_t *ids, double *sums, int64_t *counts, double *last,
+                    int32_t reset) {
+  if (!e || (count && (!ids || !sums || !counts || !last))) return SSE_ERR_ARG;
+  if (count == 0) return SSE_OK;
+  cudaSetDevice(e->device);
+  std::vector<int32_t> off(count + 1, 0);
+  for (int i = 0; i < count; i++) {
+    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+    off[i + 1] = off[i] + e->models[e->walkers[ids[i]].model].nobs;
+  }
+  const size_t tot = (size_t)off[count];
+  int32_t *d_ids = nullptr, *d_off = nullptr;
+  double *d_s = nullptr, *d_l = nullptr;
+  long long *d_c = nullptr;
+  int rc = dev_alloc(e, &d_ids, count);
+  if (!rc) rc = dev_alloc(e, &d_off, count + 1);
+  if (!rc) rc = dev_alloc(e, &d_s, tot);
+  if (!rc) rc = dev_alloc(e, &d_l, tot);
+  if (!rc) rc = dev_alloc(e, &d_c, tot);
+  if (rc) return rc;
+  CUDA_TRY(e, cudaMemcpyAsync(d_ids, ids, sizeof(int32_t) * count, cudaMemcpyHostToDevice, e->stream));
+  CUDA_TRY(e, cudaMemcpyAsync(d_off, off.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice, e->stream));
+  k_gather_obs<<<count, 64, 0, e->stream>>>(e->d_walkers, d_ids, count, d_off, d_s, d_c, d_l, reset);
+  CUDA_TRY(e, cudaGetLastError());
+  CUDA_TRY(e, cudaMemcpyAsync(sums, d_s, sizeof(double) * tot, cudaMemcpyDeviceToHost, e->stream));
+  CUDA_TRY(e, cudaMemcpyAsync(counts, d_c, sizeof(long long) * tot, cudaMemcpyDeviceToHost, e->stream));
+  CUDA_TRY(e, cudaMemcpyAsync(last, d_l, sizeof(double) * tot, cudaMemcpyDeviceToHost, e->stream));
+  dev_free(e, d_ids);
+  dev_free(e, d_off);
+  dev_free(e, d_s);
+  dev_free(e, d_l);
+  dev_free(e, d_c);
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  return SSE_OK;
+}
+
+static void info_from(const DevWalker &w, sse_walker_info *info) {
+  info->L = w.L;
+  info->num_operators = w.n;
+  info->capacity = w.cap;
+  info->sweeps = w.sweeps;
+  info->rng_counter = w.ctr;
+  info->num_worms = w.num_worms;
+  info->avg_worm_length = w.avg_len;
+  info->T = w.T;
+  info->status = w.status == ST_NEED_GROW ? SSE_OK : w.status;
+  info->model = w.model;
+  info->resize_after_thermalization = w.resize_after_therm;
+  info->slot_visits = w.slot_visits;
+  info->worm_steps = w.worm_steps;
+  for (int i = 0; i < 4; i++) info->phase_cycles[i] = w.cyc[i];
+}
+
+int sse_walker_info_get(sse_engine *e, int32_t id, sse_walker_info *info) {
+  if (!e || !info || !valid_id(e, id)) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  DevWalker w;
+  int rc = read_walker(e, id, w);
+  if (rc) return rc;
+  info_from(w, info);
+  return SSE_OK;
+}
+
+int sse_walker_export(sse_engine *e, int32_t id, uint32_t *ops, int64_t ops_len, uint8_t *state,
+                      sse_walker_info *info) {
+  if (!e || !valid_id(e, id)) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  DevWalker w;
+  int rc = read_walker(e, id, w);
+  if (rc) return rc;
+  if (ops) {
+    if (ops_len < w.L) return fail(e, SSE_ERR_ARG, "ops buffer shorter than L");
+    if (w.L) CUDA_TRY(e, cudaMemcpy(ops, w.ops, sizeof(uint32_t) * (size_t)w.L, cudaMemcpyDeviceToHost));
+  }
+  if (state) CUDA_TRY(e, cudaMemcpy(state, w.state, (size_t)e->models[w.model].nsites, cudaMemcpyDeviceToHost));
+  if (info) info_from(w, info);
+  return SSE_OK;
+}
+
+int sse_walker_import(sse_engine *e, int32_t id, const uint32_t *ops, const uint8_t *state,
+                      const sse_walker_info *info) {
+  if (!e || !info || !valid_id(e, id) || (info->L > 0 && !ops) || !state) return SSE_ERR_ARG;
+  if (info->L < 0 || info->num_operators < 0 || info->num_operators > info->L) return fail(e, SSE_ERR_ARG, "bad L/n");
+  cudaSetDevice(e->device);
+  const HostModel &hm = e->models[e->walkers[id].model];
+  long long n = 0;
+  for (long long p = 0; p < info->L; p++) {
+    const uint32_t op = ops[p];
+    if (!op) continue;
+    n++;
+    if ((int)(op >> 11) >= hm.dev.nbonds || !(op & 1u)) return fail(e, SSE_ERR_ARG, "opstring has an invalid operator");
+  }
+  if (n != info->num_operators) return fail(e, SSE_ERR_ARG, "num_operators does not match the opstring");
+  for (int i = 0; i < hm.nsites; i++)
+    if (state[i] >= 255) return fail(e, SSE_ERR_ARG, "bad spin state");
+  int rc = grow_walker(e, id, std::max<long long>(info->L, 1));
+  if (rc) return rc;
+  DevWalker w;
+  rc = read_walker(e, id, w);
+  if (rc) return rc;
+  if (info->L) CUDA_TRY(e, cudaMemcpy(w.ops, ops, sizeof(uint32_t) * (size_t)info->L, cudaMemcpyHostToDevice));
+  CUDA_TRY(e, cudaMemcpy(w.state, state, (size_t)hm.nsites, cudaMemcpyHostToDevice));
+  w.L = info->L;
+  w.n = info->num_operators;
+  w.sweeps = info->sweeps;
+  w.ctr = info->rng_counter;
+  w.num_worms = info->num_worms;
+  w.avg_len = info->avg_worm_length;
+  w.status = ST_OK;
+  w.phase = PH_READY;
+  w.warmup_done = w.warmup;
+  return write_walker(e, id, w);
+}
+
+int sse_vertex_list(sse_engine *e, int32_t id, int32_t *vertices, int32_t *v_first, int32_t *v_last) {
+  if (!e || !valid_id(e, id) || !v_first || !v_last) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  DevWalker w;
+  int rc = read_walker(e, id, w);
+  if (rc) return rc;
+  const int N = e->models[w.model].nsites;
+  int32_t *d_vl = nullptr;
+  rc = dev_alloc(e, &d_vl, (size_t)N);
+  if (rc) return rc;
+  const size_t smem = (size_t)4 * N;
+  CUDA_TRY(e, cudaFuncSetAttribute(k_link_debug, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)std::max<size_t>(smem, 48 * 1024)));
+  k_link_debug<<<1, 32, smem, e->stream>>>(e->d_models, e->d_walkers, id, d_vl);
+  CUDA_TRY(e, cudaGetLastError());
+  std::vector<Rec> rec((size_t)std::max<long long>(w.n, 1));
+  std::vector<int32_t> vf(N), vl(N);
+  CUDA_TRY(e, cudaMemcpyAsync(vl.data(), d_vl, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, e->stream));
+  CUDA_TRY(e, cudaMemcpyAsync(vf.data(), w.vfirst, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, e->stream));
+  if (w.n)
+    CUDA_TRY(e, cudaMemcpyAsync(rec.data(), w.rec, sizeof(Rec) * (size_t)w.n, cudaMemcpyDeviceToHost, e->stream));
+  dev_free(e, d_vl);
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  auto conv = [&](int32_t x) { return x < 0 ? -1 : 4 * rec[x >> 2].slot + (x & 3); };
+  if (vertices) {
+    for (long long i = 0; i < 4 * w.L; i++) vertices[i] = -1;
+    for (long long k = 0; k < w.n; k++)
+      for (int l = 0; l < 4; l++) vertices[4LL * rec[k].slot + l] = conv(rec[k].link[l]);
+  }
+  for (int i = 0; i < N; i++) {
+    v_first[i] = conv(vf[i]);
+    v_last[i] = conv(vl[i]);
+  }
+  return SSE_OK;
+}
+
+int sse_last_timing(sse_engine *e, double *ms, int64_t *launches) {
+  if (!e) return SSE_ERR_ARG;
+  if (ms) *ms = e->last_ms;
+  if (launches) *launches = e->last_launches;
+  return SSE_OK;
+}
+
+int sse_set_launch(sse_engine *e, int32_t warps_per_block, int32_t blocks_per_sm) {
+  if (!e || warps_per_block < 0 || warps_per_block > 8 || blocks_per_sm < 0) return SSE_ERR_ARG;
+  e->warps_per_block = warps_per_block;
+  e->blocks_per_sm = blocks_per_sm;
+  return SSE_OK;
+}
+
+int sse_get_launch(sse_engine *e, int32_t *warps_per_block, int32_t *blocks_per_sm) {
+  if (!e) return SSE_ERR_ARG;
+  if (warps_per_block) *warps_per_block = e->warps_per_block;
+  if (blocks_per_sm) *blocks_per_sm = e->blocks_per_sm;
+  return SSE_OK;
+}
+
+int sse_profiler_range(sse_engine *e, int32_t start) {
+  if (!e) return SSE_ERR_ARG;
+  cudaSetDevice(e->device);
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  CUDA_TRY(e, start ? cudaProfilerStart() : cudaProfilerStop());
+  return SSE_OK;
+}
+
+}  // extern "C"
