@@ -178,6 +178,76 @@ int sse_get_launch(sse_engine *eng, int32_t *warps_per_block, int32_t *blocks_pe
  * collection off; start != 0 opens the region, 0 closes it */
 int sse_profiler_range(sse_engine *eng, int32_t start);
 
+/* ---- allocation-free sweep (no counterpart in the reference) ----
+ *
+ * For callers that cannot call cudaMalloc: code that lives inside a host
+ * whose device memory belongs to someone else's pool (a Julia CUDA.jl or
+ * PyTorch caching allocator, a serving process with a fixed memory budget),
+ * and latency-critical loops that cannot afford the implicit device
+ * synchronisation of cudaMalloc/cudaFree.  The caller owns every input and
+ * output buffer in device memory; the per-sweep scratch (compacted operator
+ * records, slot index, per-site heads) and the tables derived from the model
+ * live in one static device array of about 12 MB (its size follows from the
+ * SSE_NOALLOC_MAX_* limits below), which every GPU that loads this library
+ * holds until the process exits.
+ *
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  All calls share the one array and leave the
+ * last call's contents in it; everything a call reads from it is rewritten
+ * by that call first.  Calls whose device work overlaps (several host
+ * threads, several streams) race on the array and must be serialised by the
+ * caller.  The call is synchronous and returns the walker's sse_status. */
+#define SSE_NOALLOC_MAX_SLOTS (1 << 18)    /* opstring capacity (cutoff L) */
+#define SSE_NOALLOC_MAX_SITES (1 << 14)
+#define SSE_NOALLOC_MAX_BONDS (1 << 16)
+#define SSE_NOALLOC_MAX_TYPES 64
+#define SSE_NOALLOC_MAX_VERTICES 4096      /* summed over bond types */
+#define SSE_NOALLOC_MAX_DIAG 4096          /* summed d0*d1 over bond types */
+#define SSE_NOALLOC_MAX_TRANSITIONS (1 << 16)
+#define SSE_NOALLOC_MAX_OUTCOMES (1 << 16)
+
+/* one walker for sse_sweep_noalloc, kept by the caller in device memory */
+typedef struct sse_noalloc_walker {
+  /* parameters, as sse_walker_params */
+  double T;
+  uint64_t seed;
+  uint64_t stream;
+  int64_t init_opstring_cutoff;
+  int32_t diagonal_warmup_sweeps;
+  int32_t phase;       /* 0: Carlo.init! still to run (set by the caller), 2: initialised */
+  double init_num_worms;
+  double num_worms_attenuation_factor;
+  double target_worm_length_fraction;
+  int64_t thermalization;
+  /* chain state, updated by every call */
+  int64_t L;
+  int64_t num_operators;
+  int64_t sweeps;
+  uint64_t rng_counter;
+  double num_worms;
+  double avg_worm_length;
+  int32_t warmup_done;
+  int32_t status;        /* sse_status of the last call */
+  int64_t need_capacity; /* with SSE_ERR_CAPACITY: opstring slots the walker needs next */
+  int64_t slot_visits;
+  int64_t worm_steps;
+} sse_noalloc_walker;
+
+/* Runs Carlo.init! (when walker->phase == 0) and then nsweeps Carlo steps of one walker,
+ * like sse_walkers_init + sse_sweep, without allocating anything.
+ *   model       host struct whose array pointers are DEVICE pointers to the flat tables
+ *   walker      device pointer
+ *   ops         device, ops_capacity uint32 slots (<= SSE_NOALLOC_MAX_SLOTS)
+ *   state       device, nsites uint8
+ *   obs_*       device, 6 + 5*nest entries each (accumulated, never cleared here)
+ * Sizes beyond the SSE_NOALLOC_MAX_* limits are rejected with SSE_ERR_CAPACITY.  When the
+ * reference's cutoff growth needs more than ops_capacity slots, the walker stops at a sweep
+ * boundary with status SSE_ERR_CAPACITY and need_capacity set; grow ops and call again. */
+int sse_sweep_noalloc(const sse_model_desc *model, sse_noalloc_walker *walker, uint32_t *ops,
+                      int64_t ops_capacity, uint8_t *state, double *obs_sum, int64_t *obs_count,
+                      double *obs_last, int32_t nsweeps, uint32_t flags);
+
 #ifdef __cplusplus
 }
 #endif

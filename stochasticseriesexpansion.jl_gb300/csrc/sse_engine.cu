@@ -1044,3 +1044,280 @@ int sse_profiler_range(sse_engine *e, int32_t start) {
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free sweep (sse_sweep_noalloc): the scratch of k_walk and the tables
+// derived from the model live in one static device array.
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct NoAllocScratch {
+  Rec rec[SSE_NOALLOC_MAX_SLOTS];
+  int32_t cidx[SSE_NOALLOC_MAX_SLOTS];
+  int32_t vfirst[SSE_NOALLOC_MAX_SITES];
+  int4 bond_info[SSE_NOALLOC_MAX_BONDS];
+  Trans trans[SSE_NOALLOC_MAX_TRANSITIONS];
+  Outcome outc[SSE_NOALLOC_MAX_OUTCOMES];
+  DevType types[SSE_NOALLOC_MAX_TYPES];
+  int32_t diag_vc[SSE_NOALLOC_MAX_DIAG];
+  int8_t vclass[SSE_NOALLOC_MAX_VERTICES];
+  double cls_w[128];
+  DevModel model;
+  DevWalker walker;
+  int32_t status;
+  int32_t flags[2];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// Derives the engine's model tables from the caller's flat tables (device pointers) and
+// loads the caller's walker into the scratch.  One block; writes status != 0 on overflow.
+__global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_walker *uw, uint32_t *ops,
+                               long long ops_capacity, uint8_t *state, double *obs_sum, long long *obs_count,
+                               double *obs_last) {
+  __shared__ int s_sizes[4];  // ndiag, nvert, ntrans, nout
+  __shared__ int s_ncls;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) {
+    X->status = SSE_OK;
+    int ndiag = 0, nvert = 0, ntrans = 0;
+    for (int t = 0; t < d.ntypes; t++) {
+      const int d0 = d.type_dims[2 * t], d1 = d.type_dims[2 * t + 1];
+      ndiag = max(ndiag, d.type_diag_off[t] + d0 * d1);
+      nvert = max(nvert, d.type_vert_off[t] + d.type_nverts[t]);
+      ntrans = max(ntrans, d.type_trans_off[t] + d.type_nverts[t] * 4 * d.type_maxworm[t]);
+      if (d0 < 2 || d1 < 2 || d0 > 255 || d1 > 255 || d.type_maxworm[t] < 1 || d.type_nverts[t] < 1 ||
+          d.type_nverts[t] > 512)
+        X->status = SSE_ERR_ARG;
+    }
+    s_sizes[0] = ndiag;
+    s_sizes[1] = nvert;
+    s_sizes[2] = ntrans;
+    s_sizes[3] = 0;
+  }
+  __syncthreads();
+  for (int i = tid; i < s_sizes[2]; i += nt) {
+    const int st = d.trans_start[i];
+    if (st >= 0) atomicMax(&s_sizes[3], st + d.trans_count[i]);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (s_sizes[0] > SSE_NOALLOC_MAX_DIAG || s_sizes[1] > SSE_NOALLOC_MAX_VERTICES ||
+        s_sizes[2] > SSE_NOALLOC_MAX_TRANSITIONS || s_sizes[3] > SSE_NOALLOC_MAX_OUTCOMES)
+      X->status = SSE_ERR_CAPACITY;
+    // weight classes of the diagonal vertices, in vertex order (as sse_model_register)
+    int ncls = 0;
+    for (int v = 0; v < s_sizes[1] && v < SSE_NOALLOC_MAX_VERTICES; v++) X->vclass[v] = -1;
+    if (X->status == SSE_OK) {
+      for (int t = 0; t < d.ntypes; t++) {
+        for (int v = 0; v < d.type_nverts[t]; v++) {
+          const int vo = d.type_vert_off[t] + v;
+          const uint8_t *ls = d.leg_state + 4 * vo;
+          if (ls[0] != ls[2] || ls[1] != ls[3]) continue;
+          const double w = d.weight[vo];
+          int c = 0;
+          while (c < ncls && X->cls_w[c] != w) c++;
+          if (c == ncls && ncls < 128) X->cls_w[ncls++] = w;
+          X->vclass[vo] = (int8_t)min(c, 127);
+        }
+      }
+    }
+    s_ncls = ncls;
+  }
+  __syncthreads();
+  if (X->status != SSE_OK) {
+    if (tid == 0) uw->status = X->status;
+    return;
+  }
+  for (int t = tid; t < d.ntypes; t += nt) {
+    DevType &x = X->types[t];
+    x.d0 = d.type_dims[2 * t];
+    x.d1 = d.type_dims[2 * t + 1];
+    x.nverts = d.type_nverts[t];
+    x.maxworm = d.type_maxworm[t];
+    x.diag_off = d.type_diag_off[t];
+    x.vert_off = d.type_vert_off[t];
+    x.trans_off = d.type_trans_off[t];
+    x.pad = 0;
+  }
+  for (int b = tid; b < d.nbonds; b += nt)
+    X->bond_info[b] = make_int4(d.bond_sites[2 * b], d.bond_sites[2 * b + 1], d.bond_type[b], 0);
+  for (int i = tid; i < s_sizes[0]; i += nt) {
+    const int vc = d.diag_vertex[i];
+    X->diag_vc[i] = -1;
+    if (vc < 0) continue;
+    // find the type owning entry i to locate the vertex's class
+    for (int t = 0; t < d.ntypes; t++) {
+      const int o = d.type_diag_off[t], nst = d.type_dims[2 * t] * d.type_dims[2 * t + 1];
+      if (i >= o && i < o + nst) {
+        const int cls = X->vclass[d.type_vert_off[t] + (vc >> 1)];
+        X->diag_vc[i] = cls >= 0 ? (vc | (cls << 16)) : -1;
+        break;
+      }
+    }
+  }
+  for (int o = tid; o < s_sizes[3]; o += nt) {
+    const double cum = d.out_cum[o];
+    unsigned long long thr = 0ull;
+    if (cum >= 1.0) thr = 1ull << 53;
+    else if (cum > 0.0) thr = (unsigned long long)ceil(cum * 0x1.0p53);
+    X->outc[o].thr = thr;
+    X->outc[o].packed = d.out_leg[o] | (d.out_worm[o] << 2) | (d.out_target[o] << 10);
+    X->outc[o].pad = 0;
+  }
+  __syncthreads();
+  for (int i = tid; i < s_sizes[2]; i += nt) {
+    const int st = d.trans_start[i], cnt = d.trans_count[i];
+    Trans &tr = X->trans[i];
+    if (st < 0 || cnt <= 0) {
+      tr.thr0 = 0;
+      tr.packed0 = -1;
+      tr.rest = 0;
+    } else {
+      tr.thr0 = X->outc[st].thr;
+      tr.packed0 = X->outc[st].packed;
+      tr.rest = ((st + 1) << 8) | (cnt - 1);
+    }
+  }
+  if (tid == 0) {
+    DevModel &m = X->model;
+    m.nsites = d.nsites;
+    m.nbonds = d.nbonds;
+    m.ntypes = d.ntypes;
+    m.maxdim = d.maxdim;
+    m.nest = d.nest;
+    m.nobs = 6 + 5 * d.nest;
+    m.energy_offset = d.energy_offset;
+    m.norm_site_count = d.norm_site_count;
+    m.bond_info = X->bond_info;
+    m.site_dims = d.site_dims;
+    m.types = X->types;
+    m.diag_vertex = d.diag_vertex;
+    m.weight = d.weight;
+    m.sign = d.sign;
+    m.leg_state = d.leg_state;
+    m.diag_vc = X->diag_vc;
+    m.vclass = X->vclass;
+    m.cls_w = X->cls_w;
+    m.ncls = s_ncls;
+    m.trans = X->trans;
+    m.outc = X->outc;
+    m.est_coef = d.est_coef;
+    DevWalker &w = X->walker;
+    memset(&w, 0, sizeof w);
+    w.ops = ops;
+    w.rec = X->rec;
+    w.cidx = X->cidx;
+    w.vfirst = X->vfirst;
+    w.state = state;
+    w.obs_sum = obs_sum;
+    w.obs_last = obs_last;
+    w.obs_count = obs_count;
+    w.cap = ops_capacity;
+    w.L = uw->L;
+    w.n = uw->num_operators;
+    w.ctr = uw->rng_counter;
+    w.T = uw->T;
+    w.num_worms = uw->phase == PH_NEW ? uw->init_num_worms : uw->num_worms;
+    w.avg_len = uw->phase == PH_NEW ? 1.0 : uw->avg_worm_length;
+    w.att = uw->num_worms_attenuation_factor;
+    w.target_frac = uw->target_worm_length_fraction;
+    w.seed = uw->seed;
+    w.stream = uw->stream;
+    w.therm = uw->thermalization;
+    w.sweeps = uw->sweeps;
+    long long cut = uw->init_opstring_cutoff;
+    if (cut < 0) cut = (long long)nearbyint((double)d.nsites * uw->T);
+    w.init_cutoff = cut;
+    w.slot_visits = uw->slot_visits;
+    w.worm_steps = uw->worm_steps;
+    w.model = 0;
+    w.phase = uw->phase == PH_READY ? PH_READY : (uw->phase == PH_WARMUP ? PH_WARMUP : PH_NEW);
+    w.warmup = uw->diagonal_warmup_sweeps;
+    w.warmup_done = uw->warmup_done;
+    if (w.phase == PH_NEW && cut > ops_capacity) {
+      X->status = SSE_ERR_CAPACITY;
+      uw->status = SSE_ERR_CAPACITY;
+      uw->need_capacity = cut;
+    }
+    X->flags[0] = X->flags[1] = 0;
+  }
+}
+
+// Copies the walker back to the caller and leaves its status in X->status.
+__global__ void k_noalloc_finish(NoAllocScratch *X, sse_noalloc_walker *uw) {
+  const DevWalker &w = X->walker;
+  uw->L = w.L;
+  uw->num_operators = w.n;
+  uw->sweeps = w.sweeps;
+  uw->rng_counter = w.ctr;
+  uw->num_worms = w.num_worms;
+  uw->avg_worm_length = w.avg_len;
+  uw->phase = w.phase;
+  uw->warmup_done = w.warmup_done;
+  uw->slot_visits = w.slot_visits;
+  uw->worm_steps = w.worm_steps;
+  int st = w.status;
+  if (st == ST_NEED_GROW) {
+    st = SSE_ERR_CAPACITY;
+    uw->need_capacity = w.need_L;
+  } else {
+    uw->need_capacity = 0;
+  }
+  uw->status = st;
+  X->status = st;
+}
+
+void *g_noalloc_ptr[64];
+bool g_noalloc_ready[64];
+
+}  // namespace
+
+extern "C" int sse_sweep_noalloc(const sse_model_desc *model, sse_noalloc_walker *walker, uint32_t *ops,
+                                 int64_t ops_capacity, uint8_t *state, double *obs_sum, int64_t *obs_count,
+                                 double *obs_last, int32_t nsweeps, uint32_t flags) {
+  if (!model || !walker || !ops || !state || !obs_sum || !obs_count || !obs_last || nsweeps < 0) return SSE_ERR_ARG;
+  if (ops_capacity < 1 || ops_capacity > SSE_NOALLOC_MAX_SLOTS || model->nsites < 1 ||
+      model->nsites > SSE_NOALLOC_MAX_SITES || model->nbonds < 1 || model->nbonds > SSE_NOALLOC_MAX_BONDS ||
+      model->ntypes < 1 || model->ntypes > SSE_NOALLOC_MAX_TYPES)
+    return SSE_ERR_CAPACITY;
+  if (model->maxdim < 2 || model->maxdim > 255 || model->nest < 0) return SSE_ERR_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return SSE_ERR_CUDA;
+  // once per device, with that device current: the device address of the static scratch array
+  if (!g_noalloc_ready[dev]) {
+    void *ptr = nullptr;
+    if (cudaGetSymbolAddress(&ptr, g_noalloc_scratch) != cudaSuccess || !ptr) return SSE_ERR_CUDA;
+    g_noalloc_ptr[dev] = ptr;
+    g_noalloc_ready[dev] = true;
+  }
+  NoAllocScratch *X = reinterpret_cast<NoAllocScratch *>(g_noalloc_ptr[dev]);
+  k_noalloc_prep<<<1, 256>>>(X, *model, walker, ops, (long long)ops_capacity, state, obs_sum,
+                             reinterpret_cast<long long *>(obs_count), obs_last);
+  if (cudaGetLastError() != cudaSuccess) return SSE_ERR_CUDA;
+  int st = SSE_OK;
+  if (cudaMemcpyFromSymbol(&st, g_noalloc_scratch, sizeof(int), offsetof(NoAllocScratch, status)) != cudaSuccess)
+    return SSE_ERR_CUDA;
+  if (st != SSE_OK) return st;
+  const int spw = ((std::max(4 * model->nsites, 512)) + 15) & ~15;
+  const int smem = std::max(spw, 48 * 1024);
+  const DevModel *dm = &X->model;
+  DevWalker *dw = &X->walker;
+  int *dflags = X->flags;
+  if (cudaFuncSetAttribute(k_walk<MODE_INIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
+      cudaFuncSetAttribute(k_walk<MODE_SWEEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+    return SSE_ERR_CUDA;
+  k_walk<MODE_INIT><<<1, 32, spw>>>(dm, dw, nullptr, 1, 0, nullptr, flags, -1, spw, dflags);
+  if (cudaGetLastError() != cudaSuccess) return SSE_ERR_CUDA;
+  int wst = 0;
+  if (cudaMemcpyFromSymbol(&wst, g_noalloc_scratch, sizeof(int),
+                           offsetof(NoAllocScratch, walker) + offsetof(DevWalker, status)) != cudaSuccess)
+    return SSE_ERR_CUDA;
+  if (wst == SSE_OK) k_walk<MODE_SWEEP><<<1, 32, spw>>>(dm, dw, nullptr, 1, 0, nullptr, flags, nsweeps, spw, dflags);
+  k_noalloc_finish<<<1, 1>>>(X, walker);
+  if (cudaGetLastError() != cudaSuccess) return SSE_ERR_CUDA;
+  if (cudaMemcpyFromSymbol(&st, g_noalloc_scratch, sizeof(int), offsetof(NoAllocScratch, status)) != cudaSuccess)
+    return SSE_ERR_CUDA;
+  return st;
+}

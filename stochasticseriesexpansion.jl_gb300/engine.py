@@ -77,6 +77,20 @@ class WalkerInfo(C.Structure):
         return d
 
 
+class NoAllocWalker(C.Structure):
+    """sse_noalloc_walker: one walker kept by the caller in device memory."""
+
+    _fields_ = [
+        ("T", C.c_double), ("seed", C.c_uint64), ("stream", C.c_uint64), ("init_opstring_cutoff", C.c_int64),
+        ("diagonal_warmup_sweeps", C.c_int32), ("phase", C.c_int32), ("init_num_worms", C.c_double),
+        ("num_worms_attenuation_factor", C.c_double), ("target_worm_length_fraction", C.c_double),
+        ("thermalization", C.c_int64), ("L", C.c_int64), ("num_operators", C.c_int64), ("sweeps", C.c_int64),
+        ("rng_counter", C.c_uint64), ("num_worms", C.c_double), ("avg_worm_length", C.c_double),
+        ("warmup_done", C.c_int32), ("status", C.c_int32), ("need_capacity", C.c_int64),
+        ("slot_visits", C.c_int64), ("worm_steps", C.c_int64),
+    ]
+
+
 _lib = None
 
 
@@ -109,6 +123,8 @@ def lib():
             "sse_set_launch": ([eng, I32, I32], C.c_int),
             "sse_get_launch": ([eng, P(I32), P(I32)], C.c_int),
             "sse_profiler_range": ([eng, I32], C.c_int),
+            "sse_sweep_noalloc": ([P(ModelDesc), C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_void_p, I32, U32], C.c_int),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -125,7 +141,31 @@ def exported_symbols():
         "sse_model_nobs", "sse_walkers_create", "sse_walkers_destroy", "sse_walkers_reserve", "sse_walkers_init",
         "sse_sweep", "sse_observables", "sse_walker_info_get", "sse_walker_export", "sse_walker_import",
         "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range",
+        "sse_sweep_noalloc",
     ]
+
+
+def device_model_desc(flat, device_ptr):
+    """An sse_model_desc whose array pointers are device addresses: ``device_ptr(name, array)``
+    returns the device address holding a copy of ``flat.arrays[name]`` (the caller owns that memory)."""
+    a = flat.arrays
+    q = lambda name, t: C.cast(C.c_void_p(device_ptr(name, a[name])), P(t))  # noqa: E731
+    return ModelDesc(
+        flat.nsites, flat.nbonds, flat.ntypes, flat.maxdim, flat.nest, flat.energy_offset, flat.norm_site_count,
+        q("site_dims", C.c_int32), q("bond_type", C.c_int32), q("bond_sites", C.c_int32), q("type_dims", C.c_int32),
+        q("type_nverts", C.c_int32), q("type_maxworm", C.c_int32), q("type_diag_off", C.c_int32),
+        q("type_vert_off", C.c_int32), q("type_trans_off", C.c_int32), q("diag_vertex", C.c_int32),
+        q("weight", C.c_double), q("sign", C.c_int8), q("leg_state", C.c_uint8), q("trans_start", C.c_int32),
+        q("trans_count", C.c_int32), q("out_cum", C.c_double), q("out_target", C.c_int32), q("out_leg", C.c_int8),
+        q("out_worm", C.c_int8), q("est_coef", C.c_double),
+    )
+
+
+def sweep_noalloc(desc, walker, ops, ops_capacity, state, obs_sum, obs_count, obs_last, nsweeps, flags=SSE_SWEEP_MEASURE):
+    """sse_sweep_noalloc with device addresses (ints) for every buffer; returns the sse_status."""
+    return lib().sse_sweep_noalloc(C.byref(desc), C.c_void_p(walker), C.c_void_p(ops), int(ops_capacity),
+                                   C.c_void_p(state), C.c_void_p(obs_sum), C.c_void_p(obs_count),
+                                   C.c_void_p(obs_last), int(nsweeps), int(flags))
 
 
 def _p(a, t):
