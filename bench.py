@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--side", type=int, default=32)
     ap.add_argument("--beta", type=float, default=16.0)
     ap.add_argument("--therm", type=int, default=2000, help="thermalisation sweeps before the warm-up steps")
-    ap.add_argument("--sweeps-per-step", type=int, default=20)
+    ap.add_argument("--sweeps-per-step", type=int, default=50)
     ap.add_argument("--plain-walkers", type=int, default=8)
     ap.add_argument("--cpu-sweeps", type=int, default=20, help="sweeps per chain in the CPU baseline sample")
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -342,6 +342,11 @@ def main():
         cpu = cpu_baseline(S, flat, states, args, args.cpu_threads or os.cpu_count() or 1)
 
         mean_L = float(np.mean([x["L"] for x in info1]))
+        cyc = np.array([np.array(b["phase_cycles"], dtype=float) - np.array(a["phase_cycles"], dtype=float)
+                        for a, b in zip(info0, info1)])
+        work = np.array([(b["worm_steps"] - a["worm_steps"]) + (b["slot_visits"] - a["slot_visits"])
+                         for a, b in zip(info0, info1)], dtype=float)
+        phases = dict(zip(["diagonal", "link", "worm", "measure"], (cyc.sum(0) / cyc.sum()).round(4).tolist()))
         result = {
             "metric": METRIC,
             "value": value,
@@ -367,6 +372,8 @@ def main():
                 "mean_cutoff_L": mean_L,
             },
             "operator_updates_per_s": opupd,
+            "phase_cycle_share": phases,
+            "load_balance_mean_over_max_walker_work": float(work.mean() / work.max()),
             "plain": {"value": plain_value, "unit": METRIC, "walkers": len(sub),
                       "path": "one kernel launch (one warp) per walker per sweep, synchronised after each"},
             "batched_over_plain": value / plain_value,
