@@ -56,6 +56,8 @@ struct DevModel {
   const int8_t *vclass;     // weight class of every vertex (-1: off-diagonal)
   const double *cls_w;      // weight of each class
   int32_t ncls, pad2, pad3, pad4;
+  const int32_t *est_coef2;  // 2 * est_coef as integers when est_int (every coefficient a multiple of 1/2)
+  int32_t est_int, pad5, pad6, pad7;
   const struct Trans *trans;  // one per (type, vertex, leg_in, worm_in)
   const struct Outcome *outc;
   const double *est_coef;
@@ -849,8 +851,167 @@ __device__ __forceinline__ void observe(DevWalker *W, int idx, double v) {
   W->obs_count[idx] += 1;
 }
 
+// Exact pass for models whose coefficients are multiples of 1/2 (every MagnetModel): running
+// magnetisations are integers in units of 1/2, sums are exact (m^4 in 128 bits), and the result
+// is converted to double once.  Handles estimators e0 .. e0+ne-1 (ne <= 2) and, on the first
+// pass, the sign parity.
+__device__ __forceinline__ long long warp_sum_i64(long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
+__device__ __forceinline__ unsigned __int128 warp_sum_u128(unsigned __int128 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long lo = __shfl_xor_sync(FULL, (unsigned long long)v, o);
+    const unsigned long long hi = __shfl_xor_sync(FULL, (unsigned long long)(v >> 64), o);
+    v += ((unsigned __int128)hi << 64) | lo;
+  }
+  return v;
+}
+
+__device__ __forceinline__ double u128_to_double(unsigned __int128 v) {
+  const unsigned long long hi = (unsigned long long)(v >> 64), lo = (unsigned long long)v;
+  return __dadd_rn(__dmul_rn(__ull2double_rn(hi), 0x1.0p64), __ull2double_rn(lo));
+}
+
+__device__ void finish_estimator(const DevModel &M, const Chain &c, DevWalker *W, int e, double sign, double mag,
+                                 double absmag, double mag2, double mag4) {
+  const double n = (double)c.n;
+  const double est_n = __dadd_rn(1.0, n);
+  const double norm = __ddiv_rn(1.0, M.norm_site_count);
+  const double norm2 = __dmul_rn(norm, norm);
+  mag = __dmul_rn(mag, norm);
+  absmag = __dmul_rn(absmag, norm);
+  mag2 = __dmul_rn(mag2, norm2);
+  mag4 = __dmul_rn(mag4, __dmul_rn(norm2, norm2));
+  const int base = 6 + 5 * e;
+  observe(W, base + 0, __ddiv_rn(__dmul_rn(sign, mag), est_n));
+  observe(W, base + 1, __ddiv_rn(__dmul_rn(sign, absmag), est_n));
+  observe(W, base + 2, __ddiv_rn(__dmul_rn(sign, mag2), est_n));
+  observe(W, base + 3, __ddiv_rn(__dmul_rn(sign, mag4), est_n));
+  const double chi =
+      __dmul_rn(__dmul_rn(__ddiv_rn(__ddiv_rn(__ddiv_rn(1.0, c.T), __dadd_rn(est_n, 1.0)), est_n),
+                          __dadd_rn(__dmul_rn(mag, mag), mag2)),
+                M.norm_site_count);
+  observe(W, base + 4, __dmul_rn(sign, chi));
+}
+
+__device__ void observe_base(const DevModel &M, const Chain &c, DevWalker *W, double sign) {
+  const double n = (double)c.n;
+  observe(W, 0, sign);
+  observe(W, 1, n);
+  observe(W, 2, __dmul_rn(sign, n));
+  observe(W, 3, __dmul_rn(sign, __dmul_rn(n, n)));
+  observe(W, 4, __ddiv_rn(__dmul_rn(-sign, __dadd_rn(__dmul_rn(n, c.T), M.energy_offset)), M.norm_site_count));
+}
+
+template <int NE>
+__device__ long long measure_pass_int(const DevModel &M, const Chain &c, DevWalker *W, const uint32_t *__restrict__ ops,
+                                      const uint8_t *__restrict__ state, int e0, bool count_sign, double sign_in,
+                                      int lane) {
+  const long long L = c.L;
+  const int N = M.nsites, md = M.maxdim;
+  const int4 *__restrict__ bond_info = M.bond_info;
+  const DevType *__restrict__ types = M.types;
+  const int8_t *__restrict__ vsign = M.sign;
+  const uint8_t *__restrict__ leg_state = M.leg_state;
+  const int32_t *__restrict__ cf[2];
+  int t0[2], carry[2];
+  long long s1[2], s2[2], s3[2];
+  unsigned __int128 s4[2];
+#pragma unroll
+  for (int q = 0; q < NE; q++) {
+    cf[q] = M.est_coef2 + (long long)(e0 + q) * N * md;
+    int acc = 0;
+    for (int i = lane; i < N; i += 32) acc += cf[q][(long long)i * md + state[i]];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+    t0[q] = acc;
+    carry[q] = acc;
+    s1[q] = s2[q] = s3[q] = 0;
+    s4[q] = 0;
+  }
+  long long negs = 0;
+  uint32_t op_n = (lane < L) ? ops[lane] : 0u;
+  for (long long base = 0; base < L; base += 32) {
+    const uint32_t op = op_n;
+    op_n = (base + 32 + lane < L) ? ops[base + 32 + lane] : 0u;
+    int d[2] = {0, 0};
+    if (op != 0u) {
+      const int4 bi = __ldg(bond_info + (op >> 11));
+      const int vo = types[bi.z].vert_off + (int)((op >> 1) & 0x3FFu) / 2;
+      if (count_sign) negs += vsign[vo] < 0;
+      if (!(op & 2u)) {
+        const uchar4 ls = *reinterpret_cast<const uchar4 *>(leg_state + 4 * vo);
+#pragma unroll
+        for (int q = 0; q < NE; q++) {
+          d[q] = (cf[q][(long long)bi.x * md + ls.z] - cf[q][(long long)bi.x * md + ls.x]) +
+                 (cf[q][(long long)bi.y * md + ls.w] - cf[q][(long long)bi.y * md + ls.y]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NE; q++) {
+      int x = d[q];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
+      }
+      const int t = carry[q] + x;
+      if (op != 0u) {
+        const long long tl = t;
+        s1[q] += tl;
+        s2[q] += tl < 0 ? -tl : tl;
+        const long long t2 = tl * tl;
+        s3[q] += t2;
+        s4[q] += (unsigned __int128)((unsigned long long)t2) * (unsigned long long)t2;
+      }
+      carry[q] = __shfl_sync(FULL, t, 31);
+    }
+  }
+  if (count_sign) negs = warp_sum_i64(negs);
+  const double sign = count_sign ? ((negs & 1) ? -1.0 : 1.0) : sign_in;
+  if (count_sign && lane == 0) observe_base(M, c, W, sign);
+#pragma unroll
+  for (int q = 0; q < NE; q++) {
+    const long long S1 = warp_sum_i64(s1[q]), S2 = warp_sum_i64(s2[q]), S3 = warp_sum_i64(s3[q]);
+    const unsigned __int128 S4 = warp_sum_u128(s4[q]);
+    if (lane == 0) {
+      const long long a = t0[q];
+      const long long a2 = a * a;
+      const double mag = __dmul_rn(__ll2double_rn(a + S1), 0.5);
+      const double absmag = __dmul_rn(__ll2double_rn((a < 0 ? -a : a) + S2), 0.5);
+      const double mag2 = __dmul_rn(__ll2double_rn(a2 + S3), 0.25);
+      const double mag4 = __dmul_rn(u128_to_double(S4 + (unsigned __int128)((unsigned long long)a2) * (unsigned long long)a2),
+                                    0.0625);
+      finish_estimator(M, c, W, e0 + q, sign, mag, absmag, mag2, mag4);
+    }
+  }
+  __syncwarp();
+  return (long long)(sign < 0 ? 1 : 0);
+}
+
 __device__ __noinline__ void measure(const DevModel &M, const Chain &c, DevWalker *W, const uint32_t *__restrict__ ops,
                                      const uint8_t *__restrict__ state, int lane) {
+  if (M.est_int) {
+    // one fused pass per pair of estimators; the first also measures the sign
+    double sign = 1.0;
+    if (M.nest == 0) {
+      sign = measure_pass_int<0>(M, c, W, ops, state, 0, true, 1.0, lane) ? -1.0 : 1.0;
+      return;
+    }
+    for (int e0 = 0; e0 < M.nest; e0 += 2) {
+      const bool first = e0 == 0;
+      long long neg;
+      if (M.nest - e0 >= 2) neg = measure_pass_int<2>(M, c, W, ops, state, e0, first, sign, lane);
+      else neg = measure_pass_int<1>(M, c, W, ops, state, e0, first, sign, lane);
+      if (first) sign = neg ? -1.0 : 1.0;
+    }
+    return;
+  }
   const long long L = c.L;
   long long negs = 0;
   for (long long base = 0; base < L; base += 32) {
@@ -863,14 +1024,7 @@ __device__ __noinline__ void measure(const DevModel &M, const Chain &c, DevWalke
   }
   negs = warp_sum_ll(negs);
   const double sign = (negs & 1) ? -1.0 : 1.0;
-  const double n = (double)c.n;
-  if (lane == 0) {
-    observe(W, 0, sign);
-    observe(W, 1, n);
-    observe(W, 2, __dmul_rn(sign, n));
-    observe(W, 3, __dmul_rn(sign, __dmul_rn(n, n)));
-    observe(W, 4, __ddiv_rn(__dmul_rn(-sign, __dadd_rn(__dmul_rn(n, c.T), M.energy_offset)), M.norm_site_count));
-  }
+  if (lane == 0) observe_base(M, c, W, sign);
   const int N = M.nsites, md = M.maxdim;
   for (int e = 0; e < M.nest; e++) {
     const double *coef = M.est_coef + (long long)e * N * md;
@@ -911,27 +1065,8 @@ __device__ __noinline__ void measure(const DevModel &M, const Chain &c, DevWalke
     s4 = warp_sum(s4);
     if (lane == 0) {
       const double t02 = __dmul_rn(t0, t0);
-      double mag = __dadd_rn(t0, s1);
-      double absmag = __dadd_rn(fabs(t0), s2);
-      double mag2 = __dadd_rn(t02, s3);
-      double mag4 = __dadd_rn(__dmul_rn(t02, t02), s4);
-      const double est_n = __dadd_rn(1.0, n);
-      const double norm = __ddiv_rn(1.0, M.norm_site_count);
-      const double norm2 = __dmul_rn(norm, norm);
-      mag = __dmul_rn(mag, norm);
-      absmag = __dmul_rn(absmag, norm);
-      mag2 = __dmul_rn(mag2, norm2);
-      mag4 = __dmul_rn(mag4, __dmul_rn(norm2, norm2));
-      const int base = 6 + 5 * e;
-      observe(W, base + 0, __ddiv_rn(__dmul_rn(sign, mag), est_n));
-      observe(W, base + 1, __ddiv_rn(__dmul_rn(sign, absmag), est_n));
-      observe(W, base + 2, __ddiv_rn(__dmul_rn(sign, mag2), est_n));
-      observe(W, base + 3, __ddiv_rn(__dmul_rn(sign, mag4), est_n));
-      const double chi = __dmul_rn(
-          __dmul_rn(__ddiv_rn(__ddiv_rn(__ddiv_rn(1.0, c.T), __dadd_rn(est_n, 1.0)), est_n),
-                    __dadd_rn(__dmul_rn(mag, mag), mag2)),
-          M.norm_site_count);
-      observe(W, base + 4, __dmul_rn(sign, chi));
+      finish_estimator(M, c, W, e, sign, __dadd_rn(t0, s1), __dadd_rn(fabs(t0), s2), __dadd_rn(t02, s3),
+                       __dadd_rn(__dmul_rn(t02, t02), s4));
     }
     __syncwarp();
   }

@@ -714,6 +714,20 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
   if (!rc) rc = upload(e, hm, trans.data(), ntrans, &m.trans);
   if (!rc) rc = upload(e, hm, outc.data(), nout, &m.outc);
   if (!rc) rc = upload(e, hm, d->est_coef, (size_t)d->nest * d->nsites * d->maxdim, &m.est_coef);
+  // exact integer measurement when every coefficient is a multiple of 1/2 (all MagnetModel estimators)
+  {
+    const size_t ncoef = (size_t)d->nest * d->nsites * d->maxdim;
+    std::vector<int32_t> c2(ncoef);
+    bool ok = d->nsites <= (1 << 20);
+    for (size_t i = 0; i < ncoef && ok; i++) {
+      const double x = 2.0 * d->est_coef[i];
+      if (!(std::fabs(x) <= 1024.0) || x != std::nearbyint(x)) ok = false;
+      else c2[i] = (int32_t)x;
+    }
+    m.est_int = ok ? 1 : 0;
+    if (!ok) c2.assign(1, 0);
+    if (!rc) rc = upload(e, hm, c2.data(), c2.size(), &m.est_coef2);
+  }
   if (rc) {
     for (void *p : hm.allocs) cudaFreeAsync(p, e->stream);
     return rc;
