@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--profile", action="store_true", help="open a profiler range around the timed steps only")
+    ap.add_argument("--serving-requests", type=int, default=200, help="requests in the serving run (0: skip)")
     return ap.parse_args()
 
 
@@ -204,6 +205,29 @@ def cpu_baseline(S, flat, states, args, nthreads):
     }
 
 
+def run_serving(args, device):
+    """The request loop: Poisson arrivals at 200 requests/s, continuous batching, p50/p99 time-to-result.
+    The request distribution is the serving workload's, scaled so the run is bounded: side 8-24,
+    beta 0.5-4 and 20-200 sweeps (log-uniform), 1-64 walkers, S=1/2 or 1, square or bilayer."""
+    from sse_gb300.engine import Engine
+    from sse_gb300.serving import ServingLoop, draw_requests
+
+    reqs = draw_requests(args.seed, args.serving_requests, rate=200.0, side=(8, 24), beta=(0.5, 4.0),
+                         walkers=(1, 64), sweeps=(20, 200))
+    eng = Engine(device)
+    loop = ServingLoop(eng, memory_budget=40 << 30, tick_seconds=0.25)
+    # warm the model cache (table builds are host work outside the request path)
+    for r in reqs:
+        loop._model(r.model_key)
+    loop.run(reqs, realtime=True)
+    out = loop.summary()
+    eng.close()
+    out.update(rate_per_s=200.0, distribution="side 8-24, beta 0.5-4 and sweeps 20-200 log-uniform, 1-64 walkers, "
+               "S in {1/2,1}, square or bilayer (J_perp=0.5), 20% thermalisation, 0.25 s ticks with per-walker "
+               "sweep counts sized by projected cost")
+    return out
+
+
 def run_reference(args):
     """--impl reference: the CPU implementation of the path (the oracle restatement of the
     reference's sweep; Julia is not available to run the reference itself) on all host cores."""
@@ -340,6 +364,7 @@ def main():
 
         states = [eng.export(int(i)) for i in ids[: (args.cpu_threads or os.cpu_count() or 1)]]
         cpu = cpu_baseline(S, flat, states, args, args.cpu_threads or os.cpu_count() or 1)
+        serving = run_serving(args, local) if args.serving_requests > 0 else None
 
         mean_L = float(np.mean([x["L"] for x in info1]))
         cyc = np.array([np.array(b["phase_cycles"], dtype=float) - np.array(a["phase_cycles"], dtype=float)
@@ -385,6 +410,7 @@ def main():
                     "d2h_bytes_per_step": obs_bytes},
             "gpu_launches": launches,
             "clocks": clk,
+            "serving": serving,
         }
         print(json.dumps(result), flush=True)
     eng.close()

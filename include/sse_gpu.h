@@ -151,6 +151,10 @@ int sse_walkers_init(sse_engine *eng, int32_t count, const int32_t *ids);
  *      measure! if SSE_SWEEP_MEASURE and sweeps > thermalization ---- */
 int sse_sweep(sse_engine *eng, int32_t count, const int32_t *ids, int32_t nsweeps, uint32_t flags);
 
+/* as sse_sweep, with its own number of Carlo steps for every walker (nsweeps[i] >= 0), all in one
+ * persistent launch: the continuous-batching step of a request loop */
+int sse_sweep_each(sse_engine *eng, int32_t count, const int32_t *ids, const int32_t *nsweeps, uint32_t flags);
+
 /* observable sums/counts/last values, nobs per walker, walker-major; reset clears sums and counts */
 int sse_observables(sse_engine *eng, int32_t count, const int32_t *ids, double *sums, int64_t *counts, double *last,
                     int32_t reset);

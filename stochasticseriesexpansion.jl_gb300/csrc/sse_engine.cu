@@ -91,6 +91,10 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, u
   } else {
     if (phase != PH_READY) {
       status = ST_STATE;
+    } else if (W->status != ST_OK && W->status != ST_NEED_GROW) {
+      // a walker stopped by an error (e.g. a worm that never closed) keeps its status: its
+      // opstring was left mid-update and must not be swept again
+      status = W->status;
     } else {
       long long cyc0 = 0, cyc1 = 0, cyc2 = 0, cyc3 = 0;
       while (sweeps < target) {
@@ -173,6 +177,36 @@ __global__ void __launch_bounds__(128, 7) k_walk(const DevModel *__restrict__ mo
     if (idx >= nwork) break;
     DevWalker *W = walkers + work[idx];
     process_walker<MODE>(models[W->model], W, mine, flags, add_sweeps, flag_counts, lane);
+  }
+}
+
+__global__ void k_set_targets(DevWalker *walkers, const int32_t *ids, const int32_t *nsweeps, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    DevWalker *W = walkers + ids[i];
+    W->target = W->sweeps + nsweeps[i];
+  }
+}
+
+struct GrowEntry {
+  int32_t id, pad;
+  uint32_t *ops;
+  Rec *rec;
+  int32_t *cidx;
+  long long cap;
+};
+
+// Points grown walkers at their new arrays (the host copied the opstring prefix beforehand).
+__global__ void k_apply_growth(DevWalker *walkers, const GrowEntry *g, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    DevWalker *W = walkers + g[i].id;
+    W->ops = g[i].ops;
+    W->rec = g[i].rec;
+    W->cidx = g[i].cidx;
+    W->cap = g[i].cap;
+    if (W->status == ST_NEED_GROW) W->status = ST_OK;
+    W->need_L = 0;
   }
 }
 
@@ -424,6 +458,8 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
   e->last_launches = 0;
   bool first = true;
   const bool single = (flags & SSE_SWEEP_PLAIN) && work.size() == 1;
+  int first_error = 0, failed = 0;
+  std::string err_msg;
   for (int round = 0; round < 64 && !work.empty(); round++) {
     const int n = (int)work.size();
     const int max_ns = max_nsites_of(e, n, work.data());
@@ -464,21 +500,64 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
     CUDA_TRY(e, cudaMemcpyAsync(needL.data(), e->d_needL, sizeof(long long) * n, cudaMemcpyDeviceToHost, e->stream));
     CUDA_TRY(e, cudaStreamSynchronize(e->stream));
     std::vector<int32_t> again;
+    std::vector<GrowEntry> grow;
     for (int i = 0; i < n; i++) {
       if (st[i] == ST_NEED_GROW) {
-        rc = grow_walker(e, work[i], needL[i]);
+        // new arrays for every walker that asked, copies and frees queued on the stream, then
+        // one kernel points the walkers at them
+        HostWalker &h = e->walkers[work[i]];
+        long long cap = std::max<long long>(needL[i], 2 * h.cap);
+        cap = (cap + 63) & ~63LL;
+        if (cap >= (1LL << 31) / 4) return fail(e, SSE_ERR_CAPACITY, "walker opstring exceeds 2^29 slots");
+        GrowEntry g{};
+        g.id = work[i];
+        rc = dev_alloc(e, &g.ops, (size_t)cap);
+        if (!rc) rc = dev_alloc(e, &g.rec, (size_t)cap);
+        if (!rc) rc = dev_alloc(e, &g.cidx, (size_t)cap);
         if (rc) return rc;
+        if (h.ops)
+          CUDA_TRY(e, cudaMemcpyAsync(g.ops, h.ops, sizeof(uint32_t) * (size_t)h.cap, cudaMemcpyDeviceToDevice,
+                                      e->stream));
+        dev_free(e, h.ops);
+        dev_free(e, h.rec);
+        dev_free(e, h.cidx);
+        h.ops = g.ops;
+        h.rec = g.rec;
+        h.cidx = g.cidx;
+        h.cap = cap;
+        g.cap = cap;
+        grow.push_back(g);
         again.push_back(work[i]);
       } else if (st[i] != ST_OK) {
-        char buf[128];
-        snprintf(buf, sizeof buf, "walker %d stopped with status %d", work[i], st[i]);
-        return fail(e, st[i], buf);
+        // the other walkers keep going; the failure is reported when the call returns
+        if (!first_error) {
+          first_error = st[i];
+          char buf[160];
+          snprintf(buf, sizeof buf, "walker %d stopped with status %d", work[i], st[i]);
+          err_msg = buf;
+        }
+        failed++;
       }
+    }
+    if (!grow.empty()) {
+      GrowEntry *d_g = nullptr;
+      rc = dev_alloc(e, &d_g, grow.size());
+      if (rc) return rc;
+      CUDA_TRY(e, cudaMemcpyAsync(d_g, grow.data(), sizeof(GrowEntry) * grow.size(), cudaMemcpyHostToDevice,
+                                  e->stream));
+      k_apply_growth<<<((int)grow.size() + 127) / 128, 128, 0, e->stream>>>(e->d_walkers, d_g, (int)grow.size());
+      CUDA_TRY(e, cudaGetLastError());
+      dev_free(e, d_g);
+      CUDA_TRY(e, cudaStreamSynchronize(e->stream));
     }
     work.swap(again);
   }
   if (!work.empty() && e->last_launches >= 64) return fail(e, SSE_ERR_CAPACITY, "walkers kept needing regrowth");
   e->last_ms = ms_total;
+  if (first_error) {
+    if (failed > 1) err_msg += " (" + std::to_string(failed) + " walkers failed)";
+    return fail(e, first_error, err_msg);
+  }
   return SSE_OK;
 }
 
@@ -876,6 +955,30 @@ int sse_sweep(sse_engine *e, int32_t count, const int32_t *ids, int32_t nsweeps,
     return SSE_OK;
   }
   return run_until_done(e, MODE_SWEEP, work, nsweeps, flags);
+}
+
+int sse_sweep_each(sse_engine *e, int32_t count, const int32_t *ids, const int32_t *nsweeps, uint32_t flags) {
+  if (!e || (count && (!ids || !nsweeps))) return SSE_ERR_ARG;
+  if (count == 0) return SSE_OK;
+  cudaSetDevice(e->device);
+  std::vector<int32_t> work(ids, ids + count);
+  for (int i = 0; i < count; i++) {
+    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+    if (nsweeps[i] < 0) return fail(e, SSE_ERR_ARG, "negative sweep count");
+  }
+  if (flags & SSE_SWEEP_PLAIN) return fail(e, SSE_ERR_ARG, "sse_sweep_each runs one batched launch");
+  int rc = ensure_work(e, (size_t)count);
+  if (rc) return rc;
+  int32_t *d_ns = nullptr;
+  rc = dev_alloc(e, &d_ns, (size_t)count);
+  if (rc) return rc;
+  CUDA_TRY(e, cudaMemcpyAsync(e->d_work, ids, sizeof(int32_t) * count, cudaMemcpyHostToDevice, e->stream));
+  CUDA_TRY(e, cudaMemcpyAsync(d_ns, nsweeps, sizeof(int32_t) * count, cudaMemcpyHostToDevice, e->stream));
+  k_set_targets<<<(count + 255) / 256, 256, 0, e->stream>>>(e->d_walkers, e->d_work, d_ns, count);
+  CUDA_TRY(e, cudaGetLastError());
+  dev_free(e, d_ns);
+  // targets are set: every pass keeps them (nsweeps = -1)
+  return run_until_done(e, MODE_SWEEP, work, -1, flags);
 }
 
 int sse_observables(sse_engine *e, int32_t count, const int32_t *ids, double *sums, int64_t *counts, double *last,

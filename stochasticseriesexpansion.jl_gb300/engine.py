@@ -114,6 +114,7 @@ def lib():
             "sse_walkers_reserve": ([eng, I32, P(I32), I64], C.c_int),
             "sse_walkers_init": ([eng, I32, P(I32)], C.c_int),
             "sse_sweep": ([eng, I32, P(I32), I32, U32], C.c_int),
+            "sse_sweep_each": ([eng, I32, P(I32), P(I32), U32], C.c_int),
             "sse_observables": ([eng, I32, P(I32), P(C.c_double), P(I64), P(C.c_double), I32], C.c_int),
             "sse_walker_info_get": ([eng, I32, P(WalkerInfo)], C.c_int),
             "sse_walker_export": ([eng, I32, P(U32), I64, P(C.c_uint8), P(WalkerInfo)], C.c_int),
@@ -139,7 +140,7 @@ def exported_symbols():
     return [
         "sse_abi_version", "sse_engine_create", "sse_engine_destroy", "sse_engine_last_error", "sse_model_register",
         "sse_model_nobs", "sse_walkers_create", "sse_walkers_destroy", "sse_walkers_reserve", "sse_walkers_init",
-        "sse_sweep", "sse_observables", "sse_walker_info_get", "sse_walker_export", "sse_walker_import",
+        "sse_sweep", "sse_sweep_each", "sse_observables", "sse_walker_info_get", "sse_walker_export", "sse_walker_import",
         "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range",
         "sse_sweep_noalloc",
     ]
@@ -263,6 +264,14 @@ class Engine:
         a, p = _ids(ids)
         flags = (SSE_SWEEP_MEASURE if measure else 0) | (SSE_SWEEP_PLAIN if plain else 0) | (SSE_SWEEP_GRAPH if graph else 0)
         self._check(self._L.sse_sweep(self.h, len(a), p, int(nsweeps), flags))
+
+    def sweep_each(self, ids, nsweeps, measure: bool = True):
+        """Per-walker sweep counts in one persistent launch (sse_sweep_each)."""
+        a, p = _ids(ids)
+        ns = np.ascontiguousarray(nsweeps, dtype=np.int32)
+        if len(ns) != len(a):
+            raise ValueError("one sweep count per walker")
+        self._check(self._L.sse_sweep_each(self.h, len(a), p, _p(ns, C.c_int32), SSE_SWEEP_MEASURE if measure else 0))
 
     def observables(self, ids, reset: bool = False):
         a, p = _ids(ids)

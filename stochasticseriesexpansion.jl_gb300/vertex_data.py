@@ -159,7 +159,53 @@ def vertex_apply_change(leg_states, dims, vertex, step_in, step_out):
     return int(match[0]) + 1 if len(match) else None
 
 
-def construct_transitions(weights, leg_states, max_worm_count, dims, tolerance, lp_tolerance):
+def _solve_lp(cost, A, b, lp_tolerance, lp_point):
+    """The transition LP (vertex_data.jl:267-350): min bounces s.t. A x = b, x >= 0.
+
+    lp_point = "vertex": a basic optimal solution (HiGHS simplex, like the reference's solver).
+    lp_point = "central": a point inside the optimal face (HiGHS interior point without
+    crossover), polished onto A x = b on its support.  The optimum is not unique for S >= 1;
+    vertex solutions put probability 1 on many single outcomes, and such deterministic
+    transitions can merge two worm paths into a cycle that never reaches the worm's tail (a
+    worm that never closes).  A central optimum keeps every transition that some optimal
+    solution allows, with the same (minimal) bounce weight.
+    """
+    import warnings as _w
+
+    def vertex():
+        res = linprog(cost, A_eq=A, b_eq=b, bounds=(0, None), method="highs",
+                      options={"primal_feasibility_tolerance": lp_tolerance, "dual_feasibility_tolerance": lp_tolerance})
+        if res.status != 0:
+            raise RuntimeError(f"transition probability optimization failed: {res.message}")
+        return res.x
+
+    if lp_point == "vertex":
+        return vertex()
+    x0 = vertex()
+    with _w.catch_warnings():
+        _w.simplefilter("ignore")
+        res = linprog(cost, A_eq=A, b_eq=b, bounds=(0, None), method="highs-ipm",
+                      options={"run_crossover": "off", "presolve": False, "ipm_optimality_tolerance": 1e-12,
+                               "primal_feasibility_tolerance": lp_tolerance, "dual_feasibility_tolerance": lp_tolerance})
+    if res.status != 0 or res.x is None:
+        return x0
+    x = np.where(res.x > 1e-9 * max(1.0, float(np.abs(b).max())), res.x, 0.0)
+    support = x > 0
+    if not support.any():
+        return x0
+    As = A[:, support]
+    for _ in range(3):  # least-squares projection onto A x = b on the support
+        r = b - A @ x
+        dx, *_ = np.linalg.lstsq(As, r, rcond=None)
+        x[support] += dx
+    if (x < 0).any() or np.abs(A @ x - b).max() > 1e-13 * max(1.0, float(np.abs(b).max())):
+        return x0
+    if float(cost @ x) > float(cost @ x0) + 1e-9:
+        return x0
+    return x
+
+
+def construct_transitions(weights, leg_states, max_worm_count, dims, tolerance, lp_tolerance, lp_point="vertex"):
     """vertex_data.jl:213-416."""
     nsites = len(dims)
     leg_count = 2 * nsites
@@ -229,20 +275,7 @@ def construct_transitions(weights, leg_states, max_worm_count, dims, tolerance, 
             targets[step_out] = target
             constraints[step_idx[step_out] - 1] = weights[target - 1] if target is not None else 0.0
 
-        res = linprog(
-            cost,
-            A_eq=A,
-            b_eq=constraints,
-            bounds=(0, None),
-            method="highs",
-            options={
-                "primal_feasibility_tolerance": lp_tolerance,
-                "dual_feasibility_tolerance": lp_tolerance,
-            },
-        )
-        if res.status != 0:
-            raise RuntimeError(f"transition probability optimization failed: {res.message}")
-        solution = res.x
+        solution = _solve_lp(cost, A, constraints, lp_tolerance, lp_point)
 
         for s_in in steps:
             if targets[s_in] is None:
@@ -273,6 +306,8 @@ def construct_transitions(weights, leg_states, max_worm_count, dims, tolerance, 
             transitions[(s_in[0], s_in[1], targets[s_in])] = Transition(offset, length)
             if length >= 0:
                 seg = np.cumsum(cumprobs[offset - 1 : offset + length])
+                if lp_point == "central" and abs(seg[-1] - 1) <= tolerance:
+                    seg[-1] = 1.0  # polished solutions are normalised to ~1e-13; make the row exact
                 cumprobs[offset - 1 : offset + length] = seg.tolist()
                 if abs(seg[-1] - 1) > tolerance:
                     warnings.warn(f"normalization error: {seg[-1]} != 1")
@@ -282,8 +317,16 @@ def construct_transitions(weights, leg_states, max_worm_count, dims, tolerance, 
     return transitions, cumprobs, targets_out, step_outs
 
 
-def make_vertex_data(dims, H, energy_offset_factor=0.25, tolerance=1e-7, lp_tolerance=1e-10) -> VertexData:
-    """``VertexData(dims, bond_hamiltonian; ...)`` (vertex_data.jl:48-88)."""
+def make_vertex_data(dims, H, energy_offset_factor=0.25, tolerance=1e-7, lp_tolerance=1e-10,
+                     lp_point=None) -> VertexData:
+    """``VertexData(dims, bond_hamiltonian; ...)`` (vertex_data.jl:48-88).
+
+    ``lp_point`` selects which optimal LP solution becomes the table (see ``_solve_lp``).  The
+    default, "vertex", is a basic solution from the simplex method, the kind the reference's HiGHS
+    run returns; "central" is an opt-in alternative.
+    """
+    if lp_point is None:
+        lp_point = "vertex"
     dims = tuple(int(d) for d in dims)
     H = np.asarray(H, dtype=float)
     energy_offset = calc_energy_offset(H, energy_offset_factor)
@@ -294,7 +337,7 @@ def make_vertex_data(dims, H, energy_offset_factor=0.25, tolerance=1e-7, lp_tole
     assert total_dim == H.shape[0] == H.shape[1]
     assert leg_states.shape == (2 * len(dims), len(weights))
     transitions, cum, tgt, souts = construct_transitions(
-        weights, leg_states, max_worm_count, dims, tolerance, lp_tolerance
+        weights, leg_states, max_worm_count, dims, tolerance, lp_tolerance, lp_point
     )
     return VertexData(
         energy_offset=energy_offset,

@@ -1,0 +1,78 @@
+"""Host logic of the request loop (admission by projected memory, continuous batching,
+retirement), against a fake engine: no GPU needed."""
+
+import numpy as np
+
+
+class FakeEngine:
+    def __init__(self):
+        self.next = 0
+        self.walkers = {}
+        self.models = 0
+        self.calls = []
+
+    def register_model(self, flat):
+        self.models += 1
+        return self.models - 1
+
+    def create_walkers(self, mid, params):
+        ids = np.arange(self.next, self.next + len(params), dtype=np.int32)
+        self.next += len(params)
+        for i, p in zip(ids.tolist(), params):
+            self.walkers[i] = {"sweeps": 0, "p": p}
+        return ids
+
+    def init(self, ids):
+        pass
+
+    def sweep_each(self, ids, ns, measure=True):
+        self.calls.append((list(ids), list(ns)))
+        for i, n in zip(ids.tolist(), ns.tolist()):
+            self.walkers[i]["sweeps"] += n
+
+    def observables(self, ids):
+        nobs = 16
+        return [(np.full(nobs, float(self.walkers[i]["sweeps"])), np.ones(nobs, dtype=np.int64), np.zeros(nobs))
+                for i in ids.tolist()]
+
+    def info(self, i):
+        return {"slot_visits": 10 * self.walkers[i]["sweeps"], "worm_steps": 5 * self.walkers[i]["sweeps"]}
+
+    def destroy_walkers(self, ids):
+        for i in ids.tolist():
+            del self.walkers[i]
+
+
+def test_continuous_batching_and_admission(S):
+    from sse_gb300.serving import Request, ServingLoop, projected_walker_bytes
+
+    eng = FakeEngine()
+    reqs = [Request(k, 0.0, 0.5, "square", 4, 1.0, nwalkers=2 + k % 3, nsweeps=25 + 10 * k, seed=k) for k in range(6)]
+    one = projected_walker_bytes(0.5, "square", 4, 1.0)
+    loop = ServingLoop(eng, memory_budget=6 * one, tick_sweeps=10, clock=iter(np.arange(0, 1e6, 0.5)).__next__)
+    res = loop.run(reqs, realtime=False)
+    assert sorted(r.rid for r in res) == list(range(6))
+    # every walker of every request ran exactly its sweep count
+    for r in res:
+        assert np.all(r.sums[:, 0] == reqs[r.rid].nsweeps)
+    # admission never exceeded the budget when more than one request was active
+    for ids, ns in eng.calls:
+        assert len(ids) <= 6
+        assert all(0 < n <= 10 for n in ns)
+    # later requests joined launches while earlier ones were running
+    assert any(len(set(ids)) > 2 for ids, _ in eng.calls)
+    assert not eng.walkers  # all retired
+    s = loop.summary()
+    assert s["requests"] == 6 and s["p99_s"] >= s["p50_s"] > 0
+
+
+def test_request_draw_distribution(S):
+    from sse_gb300.serving import draw_requests
+
+    reqs = draw_requests(7, 400, rate=200.0)
+    gaps = np.diff([r.arrival for r in reqs])
+    assert abs(gaps.mean() - 1 / 200) < 0.25 / 200
+    assert {r.S for r in reqs} == {0.5, 1.0} and {r.lattice for r in reqs} == {"square", "bilayer"}
+    assert all(8 <= r.side <= 64 and 0.5 <= r.beta <= 64 and 1 <= r.nwalkers <= 64 for r in reqs)
+    assert all(1000 <= r.nsweeps <= 10000 for r in reqs)
+    assert draw_requests(7, 5)[3] == draw_requests(7, 5)[3]
