@@ -175,9 +175,14 @@ int sse_vertex_list(sse_engine *eng, int32_t id, int32_t *vertices, int32_t *v_f
 /* ---- instrumentation ---- */
 /* device time (ms) of the kernels of the last sse_sweep / sse_walkers_init, and the number of kernel launches */
 int sse_last_timing(sse_engine *eng, double *ms, int64_t *launches);
-/* launch shape of the batched kernel: warps (walkers) per block; 0 = automatic */
+/* launch shape of the batched kernel: warps (walkers) per block, 1..4; 0 = automatic (4) */
 int sse_set_launch(sse_engine *eng, int32_t warps_per_block, int32_t blocks_per_sm);
 int sse_get_launch(sse_engine *eng, int32_t *warps_per_block, int32_t *blocks_per_sm);
+/* times nsweeps_probe sweeps of the given walkers with 1, 2 and 4 walkers per block and keeps the
+ * fastest launch shape; the probe sweeps are ordinary Carlo steps of those walkers (run it during
+ * thermalisation) */
+int sse_autotune(sse_engine *eng, int32_t count, const int32_t *ids, int32_t nsweeps_probe, uint32_t flags,
+                 int32_t *best_warps_per_block, double *best_ms);
 /* brackets a profiled region (cudaProfilerStart / cudaProfilerStop) for profilers started with
  * collection off; start != 0 opens the region, 0 closes it */
 int sse_profiler_range(sse_engine *eng, int32_t start);

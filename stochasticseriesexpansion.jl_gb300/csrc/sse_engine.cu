@@ -293,7 +293,11 @@ struct sse_engine {
   double last_ms = 0.0;
   long long last_launches = 0;
   int warps_per_block = 0, blocks_per_sm = 0;
-  std::map<std::pair<std::vector<int32_t>, long long>, cudaGraphExec_t> graphs;
+  struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int32_t *d_work = nullptr;
+  };
+  std::map<std::pair<std::vector<int32_t>, long long>, GraphEntry> graphs;
 };
 
 namespace {
@@ -323,6 +327,14 @@ template <class T>
 void dev_free(sse_engine *e, T *&p) {
   if (p) cudaFreeAsync(p, e->stream);
   p = nullptr;
+}
+
+void clear_graphs(sse_engine *e) {
+  for (auto &g : e->graphs) {
+    if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
+    if (g.second.d_work) cudaFreeAsync(g.second.d_work, e->stream);
+  }
+  e->graphs.clear();
 }
 
 template <class T>
@@ -473,10 +485,42 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
       CUDA_TRY(e, cudaMemcpyAsync(e->d_work, work.data(), sizeof(int32_t) * work.size(), cudaMemcpyHostToDevice,
                                   e->stream));
     }
-    CUDA_TRY(e, cudaMemsetAsync(e->d_flags, 0, 2 * sizeof(int), e->stream));
-    CUDA_TRY(e, cudaEventRecord(e->ev0, e->stream));
-    rc = launch_pass(e, mode, n, single ? work[0] : -1, flags, (mode == MODE_SWEEP && first) ? nsweeps : -1, max_ns);
-    if (rc) return rc;
+    const long long add = (mode == MODE_SWEEP && first) ? nsweeps : -1;
+    if (!single && mode == MODE_SWEEP && first && (flags & SSE_SWEEP_GRAPH)) {
+      // a sweep block replayed from a captured graph: flag and queue resets plus the persistent launch
+      auto key = std::make_pair(work, add * 4 + (long long)(flags & SSE_SWEEP_MEASURE));
+      auto it = e->graphs.find(key);
+      if (it == e->graphs.end()) {
+        if (e->graphs.size() >= 16) clear_graphs(e);
+        sse_engine::GraphEntry g;
+        rc = dev_alloc(e, &g.d_work, work.size());
+        if (rc) return rc;
+        CUDA_TRY(e, cudaMemcpyAsync(g.d_work, work.data(), sizeof(int32_t) * work.size(), cudaMemcpyHostToDevice,
+                                    e->stream));
+        CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+        int wpb, grid, spw;
+        rc = choose_launch(e, max_ns, n, wpb, grid, spw, false);
+        if (rc) return rc;
+        cudaGraph_t graph;
+        CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
+        cudaMemsetAsync(e->d_flags, 0, 2 * sizeof(int), e->stream);
+        cudaMemsetAsync(e->d_queue, 0, sizeof(int), e->stream);
+        k_walk<MODE_SWEEP><<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(
+            e->d_models, e->d_walkers, g.d_work, n, -1, e->d_queue, flags, add, spw, e->d_flags);
+        CUDA_TRY(e, cudaStreamEndCapture(e->stream, &graph));
+        CUDA_TRY(e, cudaGraphInstantiate(&g.exec, graph, 0));
+        cudaGraphDestroy(graph);
+        it = e->graphs.emplace(key, g).first;
+      }
+      CUDA_TRY(e, cudaEventRecord(e->ev0, e->stream));
+      CUDA_TRY(e, cudaGraphLaunch(it->second.exec, e->stream));
+      e->last_launches += 1;
+    } else {
+      CUDA_TRY(e, cudaMemsetAsync(e->d_flags, 0, 2 * sizeof(int), e->stream));
+      CUDA_TRY(e, cudaEventRecord(e->ev0, e->stream));
+      rc = launch_pass(e, mode, n, single ? work[0] : -1, flags, add, max_ns);
+      if (rc) return rc;
+    }
     first = false;
     CUDA_TRY(e, cudaEventRecord(e->ev1, e->stream));
     int flags_h[2];
@@ -563,6 +607,7 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
 
 int upload_models(sse_engine *e) {
   if (e->models.size() > e->d_models_cap) {
+    clear_graphs(e);
     dev_free(e, e->d_models);
     size_t cap = std::max<size_t>(8, 2 * e->models.size());
     int rc = dev_alloc(e, &e->d_models, cap);
@@ -589,8 +634,7 @@ int ensure_walker_slots(sse_engine *e, size_t n) {
   dev_free(e, e->d_walkers);
   e->d_walkers = nw;
   e->d_walkers_cap = cap;
-  for (auto &g : e->graphs) cudaGraphExecDestroy(g.second);
-  e->graphs.clear();
+  clear_graphs(e);
   return SSE_OK;
 }
 
@@ -637,7 +681,7 @@ int sse_engine_create(int32_t device, sse_engine **out) {
 int sse_engine_destroy(sse_engine *e) {
   if (!e) return SSE_ERR_ARG;
   cudaSetDevice(e->device);
-  for (auto &g : e->graphs) cudaGraphExecDestroy(g.second);
+  clear_graphs(e);
   for (auto &w : e->walkers) {
     dev_free(e, w.ops);
     dev_free(e, w.rec);
@@ -906,8 +950,7 @@ int sse_walkers_destroy(sse_engine *e, int32_t count, const int32_t *ids) {
     dev_free(e, h.obs_count);
     h.alive = false;
   }
-  for (auto &g : e->graphs) cudaGraphExecDestroy(g.second);
-  e->graphs.clear();
+  clear_graphs(e);
   CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   return SSE_OK;
 }
@@ -1139,9 +1182,33 @@ int sse_last_timing(sse_engine *e, double *ms, int64_t *launches) {
 }
 
 int sse_set_launch(sse_engine *e, int32_t warps_per_block, int32_t blocks_per_sm) {
-  if (!e || warps_per_block < 0 || warps_per_block > 8 || blocks_per_sm < 0) return SSE_ERR_ARG;
+  if (!e || warps_per_block < 0 || warps_per_block > 4 || blocks_per_sm < 0) return SSE_ERR_ARG;
+  if (warps_per_block != e->warps_per_block || blocks_per_sm != e->blocks_per_sm) clear_graphs(e);
   e->warps_per_block = warps_per_block;
   e->blocks_per_sm = blocks_per_sm;
+  return SSE_OK;
+}
+
+int sse_autotune(sse_engine *e, int32_t count, const int32_t *ids, int32_t nsweeps_probe, uint32_t flags,
+                 int32_t *best_warps_per_block, double *best_ms) {
+  if (!e || count <= 0 || !ids || nsweeps_probe <= 0) return SSE_ERR_ARG;
+  const int candidates[3] = {1, 2, 4};
+  int best = 0;
+  double best_t = 0.0;
+  for (int c : candidates) {
+    int rc = sse_set_launch(e, c, 0);
+    if (rc) return rc;
+    rc = sse_sweep(e, count, ids, nsweeps_probe, flags & SSE_SWEEP_MEASURE);
+    if (rc) return rc;
+    if (!best || e->last_ms < best_t) {
+      best = c;
+      best_t = e->last_ms;
+    }
+  }
+  int rc = sse_set_launch(e, best, 0);
+  if (rc) return rc;
+  if (best_warps_per_block) *best_warps_per_block = best;
+  if (best_ms) *best_ms = best_t;
   return SSE_OK;
 }
 

@@ -124,6 +124,7 @@ def lib():
             "sse_set_launch": ([eng, I32, I32], C.c_int),
             "sse_get_launch": ([eng, P(I32), P(I32)], C.c_int),
             "sse_profiler_range": ([eng, I32], C.c_int),
+            "sse_autotune": ([eng, I32, P(I32), I32, U32, P(I32), P(C.c_double)], C.c_int),
             "sse_sweep_noalloc": ([P(ModelDesc), C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p, I32, U32], C.c_int),
         }
@@ -141,7 +142,7 @@ def exported_symbols():
         "sse_abi_version", "sse_engine_create", "sse_engine_destroy", "sse_engine_last_error", "sse_model_register",
         "sse_model_nobs", "sse_walkers_create", "sse_walkers_destroy", "sse_walkers_reserve", "sse_walkers_init",
         "sse_sweep", "sse_sweep_each", "sse_observables", "sse_walker_info_get", "sse_walker_export", "sse_walker_import",
-        "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range",
+        "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range", "sse_autotune",
         "sse_sweep_noalloc",
     ]
 
@@ -329,6 +330,15 @@ class Engine:
         n = C.c_int64()
         self._check(self._L.sse_last_timing(self.h, C.byref(ms), C.byref(n)))
         return ms.value, n.value
+
+    def autotune(self, ids, nsweeps_probe: int = 5, measure: bool = False):
+        """Pick the fastest walkers-per-block for these walkers (the probe sweeps are real Carlo steps)."""
+        a, p = _ids(ids)
+        best = C.c_int32()
+        ms = C.c_double()
+        self._check(self._L.sse_autotune(self.h, len(a), p, int(nsweeps_probe), SSE_SWEEP_MEASURE if measure else 0,
+                                         C.byref(best), C.byref(ms)))
+        return best.value, ms.value
 
     def profiler_range(self, start: bool):
         self._check(self._L.sse_profiler_range(self.h, int(bool(start))))
