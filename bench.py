@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--profile", action="store_true", help="open a profiler range around the timed steps only")
     ap.add_argument("--serving-requests", type=int, default=200, help="requests in the serving run (0: skip)")
+    ap.add_argument("--workload", default="uniform", choices=["uniform", "single", "uneven", "bilayer"],
+                    help="uniform: the headline batch; single: one 8x8 walker at beta=2; uneven: 8192 walkers of "
+                         "mixed sizes and temperatures; bilayer: 2048 S=1 bilayer walkers 48x48")
     return ap.parse_args()
 
 
@@ -269,10 +272,112 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def sweep_tolerant(eng, ids, nsweeps, measure=True, graph=False):
+    """sse_sweep over a batch; walkers stopped by an error (a worm that never closed) are dropped
+    from the batch and counted, the others continue."""
+    from sse_gb300.engine import SSEError
+
+    try:
+        eng.sweep(ids, nsweeps, measure=measure, graph=graph)
+        return ids, 0
+    except SSEError:
+        ok = np.array([i for i in ids.tolist() if eng.info(i)["status"] == 0], dtype=np.int32)
+        return ok, len(ids) - len(ok)
+
+
+def run_other_workload(args):
+    """The other configurations, each printed as its own JSON line (not the headline line)."""
+    S = _sse_loader.load()
+    from sse_gb300.engine import Engine
+    from sse_gb300.serving import model_params
+
+    eng = Engine(0)
+    rng = np.random.default_rng(args.seed)
+    line = {"workload": args.workload}
+    if args.workload == "single":
+        # one walker, 8x8 S=1/2 Heisenberg, beta=2: persistent launch vs one launch per sweep vs the CPU oracle
+        from oracle import oracle as O
+
+        flat = S.flatten_model(make_model(S, 8))
+        mid = eng.register_model(flat)
+        a, b = eng.create_walkers(mid, [dict(T=0.5, seed=args.seed, stream=0, thermalization=10**4)] * 2)
+        eng.init([a, b])
+        eng.sweep([a, b], 2000, measure=False)
+        n = 20000
+        eng.sweep([a], n, measure=True)
+        ms, _ = eng.last_timing()
+        t0 = time.perf_counter()
+        eng.sweep([b], 500, measure=True, plain=True)
+        plain_s = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        eng.sweep([b], 500, measure=True, graph=True)
+        om = O.OracleModel(flat)
+        w = O.OracleWalker(om, T=0.5, seed=args.seed, stream=0, thermalization=10**4)
+        w.init()
+        w.run(2000, measure=False)
+        t0 = time.perf_counter()
+        w.run(n, measure=True)
+        cpu_s = time.perf_counter() - t0
+        line.update(config="8x8 S=1/2 Heisenberg, beta=2, one walker", gpu_persistent_sweeps_per_s=n / (ms / 1e3),
+                    gpu_plain_sweeps_per_s=500 / plain_s, cpu_oracle_one_core_sweeps_per_s=n / cpu_s,
+                    mean_L=eng.info(int(a))["L"])
+    elif args.workload in ("uneven", "bilayer"):
+        groups = []
+        if args.workload == "uneven":
+            sides, betas = [8, 16, 24, 32, 48, 64], [0.5, 1, 2, 4, 8, 16, 32, 64]
+            nw = 8192
+            pick = [(int(rng.choice(sides)), float(rng.choice(betas))) for _ in range(nw)]
+            models = {L: eng.register_model(S.flatten_model(make_model(S, L))) for L in sides}
+            params = [(models[L], dict(T=1.0 / b, seed=args.seed, stream=k, thermalization=10**9))
+                      for k, (L, b) in enumerate(pick)]
+            desc = "8192 walkers, S=1/2 Heisenberg square L in {8..64}, beta in {0.5..64} uniform from a seed"
+        else:
+            p = {"lattice": {"unitcell": S.UnitCells.square_bilayer, "size": (48, 48)}, "S": 1.0, "J": 1.0, "Jp": 0.5,
+                 "parameter_map": {"J": ["Jp", "J", "J", "J", "J"]}, "Dz": 0.3, "hz": 0.2, "measure": ["magnetization"]}
+            mid = eng.register_model(S.flatten_model(S.MagnetModel(p)))
+            betas = [4.0, 8.0, 16.0]
+            params = [(mid, dict(T=1.0 / betas[k % 3], seed=args.seed, stream=k, thermalization=10**9))
+                      for k in range(2048)]
+            desc = "2048 walkers, S=1 square bilayer 48x48, J=1, J_perp=0.5, Dz=0.3, hz=0.2, beta in {4,8,16}"
+        ids = []
+        for m in sorted({m for m, _ in params}):
+            ids += eng.create_walkers(m, [q for mm, q in params if mm == m]).tolist()
+        ids = np.array(ids, dtype=np.int32)
+        eng.init(ids)
+        failed = 0
+        done = 0
+        t0 = time.perf_counter()
+        while done < args.therm:
+            ids, f = sweep_tolerant(eng, ids, min(25, args.therm - done), measure=False)
+            failed += f
+            done += min(25, args.therm - done)
+        therm_s = time.perf_counter() - t0
+        info0 = {i: eng.info(i) for i in ids.tolist()}
+        t_dev = 0.0
+        for _ in range(args.steps):
+            ids, f = sweep_tolerant(eng, ids, args.sweeps_per_step, measure=True)
+            failed += f
+            t_dev += eng.last_timing()[0] / 1e3
+        info1 = {i: eng.info(i) for i in ids.tolist()}
+        ws = len(ids) * args.sweeps_per_step * args.steps
+        ou = sum(info1[i]["slot_visits"] + info1[i]["worm_steps"] - info0[i]["slot_visits"] - info0[i]["worm_steps"]
+                 for i in ids.tolist())
+        Ls = np.array([info1[i]["L"] for i in ids.tolist()])
+        line.update(config=desc, thermalization_sweeps=args.therm, thermalization_seconds=therm_s,
+                    sweeps_per_step=args.sweeps_per_step, steps=args.steps, walker_sweeps_per_s=ws / t_dev,
+                    operator_updates_per_s=ou / t_dev, walkers_stopped_by_worm_cap=failed,
+                    cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
+    eng.close()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload != "uniform":
+        run_other_workload(args)
         return
     rank, world, local = dist_setup(args)
     S = _sse_loader.load()
