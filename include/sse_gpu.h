@@ -187,6 +187,37 @@ int sse_autotune(sse_engine *eng, int32_t count, const int32_t *ids, int32_t nsw
  * collection off; start != 0 opens the region, 0 closes it */
 int sse_profiler_range(sse_engine *eng, int32_t start);
 
+/* ---- parallel tempering between resident walkers (src/sse.jl:390-405) ----
+ *
+ * Carlo.parallel_tempering_change_parameter!(mc, :T, T): sets the walker's temperature. */
+int sse_walker_set_T(sse_engine *eng, int32_t id, double T);
+
+/* One exchange step over nladders ladders of nrungs walkers (2 <= nrungs <= 1024); ladder l is
+ * ids[l*nrungs .. l*nrungs + nrungs - 1] in any order, all of one model, with distinct temperatures;
+ * a walker may appear in one ladder only.  Within a ladder the walkers are ranked by their current T
+ * (ascending) and `step` proposes the rung pairs (k, k+1) with k = step (mod 2).  For a pair (a, b),
+ * T_a < T_b, the swap weight is exp(lwr(a, T_b) + lwr(b, T_a)) with Carlo's
+ * parallel_tempering_log_weight_ratio lwr(mc, T') = -num_operators * log(T'/T), i.e.
+ * q = (T_a/T_b)^(n_a - n_b), computed as an integer power by binary powering of the correctly
+ * rounded quotient (T_a/T_b if n_a >= n_b, else T_b/T_a).  The swap is accepted when u < q with
+ * u = (x >> 11) * 2^-53, x = words (0,1) of Philox4x32-10(counter = (step, k, l), key = seed).
+ * An accepted swap exchanges the two walkers' temperatures and their observable accumulators
+ * (sums, counts, last values), so a walker's accumulators always hold the measurements taken at
+ * its current temperature.  Pairs with a walker whose status is not SSE_OK are not proposed.
+ * accepted (may be NULL): nladders*(nrungs-1) entries, pair k of ladder l at l*(nrungs-1) + k:
+ * 1 accepted, 0 rejected, -1 not proposed. */
+int sse_tempering_exchange(sse_engine *eng, int32_t nladders, int32_t nrungs, const int32_t *ids, uint64_t seed,
+                           uint64_t step, int32_t *accepted);
+
+/* nblocks times: `interval` Carlo steps of every ladder walker (as sse_sweep with `flags`), then
+ * sse_tempering_exchange with step first_step + block.  accepted_counts / proposed_counts (may be
+ * NULL): nladders*(nrungs-1) entries, this call's accepted and proposed swaps per rung pair.
+ * A walker that stops (SSE_ERR_WORM_CAP, SSE_ERR_INVALID_VERTEX) leaves the others running; the
+ * call then returns its status after the last block. */
+int sse_sweep_tempering(sse_engine *eng, int32_t nladders, int32_t nrungs, const int32_t *ids, int32_t nblocks,
+                        int32_t interval, uint64_t seed, uint64_t first_step, uint32_t flags,
+                        int64_t *accepted_counts, int64_t *proposed_counts);
+
 /* ---- allocation-free sweep (no counterpart in the reference) ----
  *
  * For callers that cannot call cudaMalloc: code that lives inside a host

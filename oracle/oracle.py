@@ -123,6 +123,10 @@ def lib():
         L.orc_draw.argtypes = [C.c_uint64, C.c_uint64, C.c_uint64]
         L.orc_tanh.restype = C.c_double
         L.orc_tanh.argtypes = [C.c_double]
+        L.orc_tempering_weight.restype = C.c_double
+        L.orc_tempering_weight.argtypes = [C.c_double, C.c_double, C.c_int64, C.c_int64]
+        L.orc_tempering_exchange.restype = C.c_int
+        L.orc_tempering_exchange.argtypes = [P(P(OrcWalker)), C.c_int32, C.c_int32, C.c_uint64, C.c_uint64, P(C.c_int32)]
         for f in ("orc_init", "orc_sweep", "orc_measure", "orc_step", "orc_run", "orc_diagonal_update",
                   "orc_make_vertex_list", "orc_worm_update", "orc_set_opstring", "orc_set_state", "orc_run_parallel"):
             getattr(L, f).restype = C.c_int
@@ -248,6 +252,19 @@ def run_parallel(model: OracleModel, walkers, nsteps, measure=True, nthreads=1):
     rc = lib().orc_run_parallel(model.ref, arr, len(walkers), nsteps, int(measure), nthreads)
     if rc != 0:
         raise RuntimeError(f"oracle error {rc}")
+
+
+def tempering_exchange(walkers, nladders, nrungs, seed, step):
+    """One parallel-tempering exchange step over ladders of oracle walkers (walkers[l*nrungs + k]);
+    returns the accept flags per rung pair, shape (nladders, nrungs - 1), and the status."""
+    arr = (P(OrcWalker) * len(walkers))(*[w.p for w in walkers])
+    acc = np.zeros(nladders * (nrungs - 1), np.int32)
+    rc = lib().orc_tempering_exchange(arr, nladders, nrungs, seed, step, _ptr(acc, C.c_int32))
+    return acc.reshape(nladders, nrungs - 1), rc
+
+
+def tempering_weight(Ta, Tb, na, nb):
+    return lib().orc_tempering_weight(Ta, Tb, na, nb)
 
 
 def philox(ctr, key):

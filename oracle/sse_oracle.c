@@ -544,3 +544,88 @@ int orc_run_parallel(const orc_model *m, orc_walker **ws, int32_t nwalkers, int6
   free(args);
   return rc;
 }
+
+/* ------------------------------------------------------------------------ */
+/* parallel tempering: Carlo.parallel_tempering_log_weight_ratio and         */
+/* parallel_tempering_change_parameter! (src/sse.jl:390-405)                 */
+/* ------------------------------------------------------------------------ */
+
+/* exp(lwr(a, T_b) + lwr(b, T_a)), lwr(mc, T') = -n log(T'/T) (src/sse.jl:390-396), written as the
+ * integer power (T_a/T_b)^(n_a - n_b) and evaluated by binary powering */
+double orc_tempering_weight(double Ta, double Tb, int64_t na, int64_t nb) {
+  uint64_t e;
+  double b;
+  if (na >= nb) {
+    e = (uint64_t)(na - nb);
+    b = Ta / Tb;
+  } else {
+    e = (uint64_t)(nb - na);
+    b = Tb / Ta;
+  }
+  double q = 1.0;
+  while (e) {
+    if (e & 1u) q = q * b;
+    e >>= 1;
+    if (e) b = b * b;
+  }
+  return q;
+}
+
+int orc_tempering_exchange(orc_walker **ws, int32_t nladders, int32_t nrungs, uint64_t seed, uint64_t step,
+                           int32_t *accepted) {
+  if (nrungs < 2) return ORC_ERR_ARG;
+  int32_t *order = (int32_t *)malloc(sizeof(int32_t) * (size_t)nrungs);
+  if (!order) return ORC_ERR_NOMEM;
+  int rc = ORC_OK;
+  for (int32_t l = 0; l < nladders; l++) {
+    orc_walker **lw = ws + (size_t)l * nrungs;
+    int32_t *acc = accepted + (size_t)l * (nrungs - 1);
+    /* rank the ladder by temperature (insertion sort), distinct temperatures required */
+    int dup = 0;
+    for (int32_t k = 0; k < nrungs; k++) {
+      int32_t j = k;
+      while (j > 0 && lw[order[j - 1]]->T > lw[k]->T) {
+        order[j] = order[j - 1];
+        j--;
+      }
+      order[j] = k;
+    }
+    for (int32_t k = 0; k + 1 < nrungs; k++)
+      if (lw[order[k]]->T == lw[order[k + 1]]->T) dup = 1;
+    for (int32_t k = 0; k + 1 < nrungs; k++) acc[k] = -1;
+    if (dup) {
+      rc = ORC_ERR_ARG;
+      continue;
+    }
+    for (int32_t k = (int32_t)(step & 1u); k + 1 < nrungs; k += 2) {
+      orc_walker *a = lw[order[k]], *b = lw[order[k + 1]];
+      if (a->status != ORC_OK || b->status != ORC_OK) continue;
+      const double q = orc_tempering_weight(a->T, b->T, a->num_operators, b->num_operators);
+      const uint32_t ctr[4] = {(uint32_t)step, (uint32_t)(step >> 32), (uint32_t)k, (uint32_t)l};
+      const uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+      uint32_t x[4];
+      orc_philox4x32_10(ctr, key, x);
+      const double u = (double)((((uint64_t)x[1] << 32) | x[0]) >> 11) * 0x1.0p-53;
+      acc[k] = u < q;
+      if (acc[k]) {
+        /* parallel_tempering_change_parameter! on both walkers (src/sse.jl:399-405); the
+         * observable accumulators stay with their temperature */
+        const double t = a->T;
+        a->T = b->T;
+        b->T = t;
+        for (int32_t i = 0; i < a->nobs; i++) {
+          const double s = a->obs_sum[i], z = a->obs_last[i];
+          const int64_t c = a->obs_count[i];
+          a->obs_sum[i] = b->obs_sum[i];
+          a->obs_last[i] = b->obs_last[i];
+          a->obs_count[i] = b->obs_count[i];
+          b->obs_sum[i] = s;
+          b->obs_last[i] = z;
+          b->obs_count[i] = c;
+        }
+      }
+    }
+  }
+  free(order);
+  return rc;
+}

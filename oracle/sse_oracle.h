@@ -34,6 +34,7 @@ extern "C" {
 
 enum {
   ORC_OK = 0,
+  ORC_ERR_ARG = 1,
   ORC_ERR_INVALID_VERTEX = 4,
   ORC_ERR_WORM_CAP = 8,
   ORC_ERR_NOMEM = 6,
@@ -118,6 +119,16 @@ int orc_set_state(const orc_model *m, orc_walker *w, const uint8_t *state);
 /* independent chains, one per thread (CPU baseline) */
 int orc_run_parallel(const orc_model *m, orc_walker **ws, int32_t nwalkers, int64_t nsteps,
                      int32_t do_measure, int32_t nthreads);
+
+/* Parallel-tempering exchange step over nladders ladders of nrungs walkers (ws[l*nrungs + k]):
+ * walkers ranked by T; step proposes rung pairs (k, k+1) with k = step mod 2; the swap weight is
+ * exp of the summed log weight ratios of src/sse.jl:390-396, q = (T_a/T_b)^(n_a - n_b) by binary
+ * powering; accept when u < q, u from Philox(counter = (step, k, l), key = seed) words 0,1; an
+ * accepted swap exchanges T and the observable accumulators.  accepted: nladders*(nrungs-1)
+ * entries, 1/0, or -1 for pairs not proposed. */
+double orc_tempering_weight(double Ta, double Tb, int64_t na, int64_t nb);
+int orc_tempering_exchange(orc_walker **ws, int32_t nladders, int32_t nrungs, uint64_t seed, uint64_t step,
+                           int32_t *accepted);
 
 /* replay stream primitives (tests) */
 void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);

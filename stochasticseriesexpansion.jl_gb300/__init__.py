@@ -18,4 +18,4 @@ from .magnet import (
 )
 from .tables import FlatModel, flatten_model, flatten_sse_data
 from . import engine
-from .mc import MC, MCContext, BatchMC
+from .mc import MC, MCContext, BatchMC, TemperingMC

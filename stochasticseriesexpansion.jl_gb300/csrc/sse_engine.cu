@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -243,6 +244,103 @@ __global__ void k_gather_obs(DevWalker *walkers, const int32_t *ids, int n, cons
       W->obs_sum[i] = 0.0;
       W->obs_count[i] = 0;
     }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// parallel tempering: Carlo.parallel_tempering_log_weight_ratio and
+// parallel_tempering_change_parameter! (src/sse.jl:390-405)
+// ---------------------------------------------------------------------------
+
+constexpr int PT_MAX_RUNGS = 1024;
+
+// exp(lwr(a, T_b) + lwr(b, T_a)) with lwr(mc, T') = -n log(T'/T), i.e. (T_a/T_b)^(n_a - n_b), as an
+// integer power by binary powering of a correctly rounded base (the same products on any IEEE-754
+// machine, so the accept decision replays exactly)
+__device__ double pt_swap_weight(double Ta, double Tb, long long na, long long nb) {
+  const bool up = na >= nb;
+  unsigned long long e = up ? (unsigned long long)(na - nb) : (unsigned long long)(nb - na);
+  double b = up ? __ddiv_rn(Ta, Tb) : __ddiv_rn(Tb, Ta);
+  double q = 1.0;
+  while (e) {
+    if (e & 1ull) q = __dmul_rn(q, b);
+    e >>= 1;
+    if (e) b = __dmul_rn(b, b);
+  }
+  return q;
+}
+
+// One block per ladder of `nrungs` walkers (ids[l*nrungs + k], any order).  The walkers are ranked by
+// their current T; step s proposes the rung pairs (k, k+1) with k = s mod 2 (mod 2), accepts one with
+// probability min(1, q) using u = rand() from Philox(counter = (s, k, l), key = seed), and exchanges
+// the two temperatures together with the observable accumulators, which stay with their temperature.
+__global__ void __launch_bounds__(256) k_tempering(DevWalker *walkers, const DevModel *models, const int32_t *ids,
+                                                   int nrungs, unsigned long long seed, unsigned long long step,
+                                                   int32_t *accepted, long long *acc_count, long long *prop_count,
+                                                   int *err) {
+  __shared__ double uT[PT_MAX_RUNGS], sT[PT_MAX_RUNGS];
+  __shared__ long long sN[PT_MAX_RUNGS];
+  __shared__ int32_t sW[PT_MAX_RUNGS];
+  __shared__ int dup;
+  const int l = blockIdx.x;
+  const int32_t *lid = ids + (size_t)l * nrungs;
+  if (threadIdx.x == 0) dup = 0;
+  for (int k = threadIdx.x; k < nrungs; k += blockDim.x) uT[k] = walkers[lid[k]].T;
+  __syncthreads();
+  for (int k = threadIdx.x; k < nrungs; k += blockDim.x) {
+    const double t = uT[k];
+    int r = 0;
+    bool same = false;
+    for (int j = 0; j < nrungs; j++) {
+      r += uT[j] < t;
+      same |= (j != k) && (uT[j] == t);
+    }
+    if (same) dup = 1;
+    else {
+      sT[r] = t;
+      sN[r] = walkers[lid[k]].n;
+      sW[r] = lid[k];
+    }
+  }
+  __syncthreads();
+  const size_t base = (size_t)l * (nrungs - 1);
+  if (dup) {
+    if (threadIdx.x == 0) atomicExch(err, 1);
+    for (int k = threadIdx.x; k < nrungs - 1; k += blockDim.x) accepted[base + k] = -1;
+    return;
+  }
+  for (int k = threadIdx.x; k < nrungs - 1; k += blockDim.x) {
+    int32_t res = -1;
+    if ((unsigned long long)(k & 1) == (step & 1ull)) {
+      DevWalker *A = walkers + sW[k], *B = walkers + sW[k + 1];
+      const bool ok = (A->status == ST_OK || A->status == ST_NEED_GROW) &&
+                      (B->status == ST_OK || B->status == ST_NEED_GROW);
+      if (ok) {
+        const double q = pt_swap_weight(sT[k], sT[k + 1], sN[k], sN[k + 1]);
+        const uint4 x = philox_block(seed, ((unsigned long long)(unsigned)l << 32) | (unsigned)k, step);
+        const unsigned long long u64 = ((unsigned long long)x.y << 32) | x.x;
+        const double u = (double)(u64 >> 11) * 0x1.0p-53;
+        res = u < q ? 1 : 0;
+        if (res) {
+          A->T = sT[k + 1];
+          B->T = sT[k];
+          const int nobs = models[A->model].nobs;
+          for (int i = 0; i < nobs; i++) {
+            const double s = A->obs_sum[i], z = A->obs_last[i];
+            const long long c = A->obs_count[i];
+            A->obs_sum[i] = B->obs_sum[i];
+            A->obs_last[i] = B->obs_last[i];
+            A->obs_count[i] = B->obs_count[i];
+            B->obs_sum[i] = s;
+            B->obs_last[i] = z;
+            B->obs_count[i] = c;
+          }
+        }
+        prop_count[base + k] += 1;
+        acc_count[base + k] += res;
+      }
+    }
+    accepted[base + k] = res;
   }
 }
 
@@ -1224,6 +1322,176 @@ int sse_profiler_range(sse_engine *e, int32_t start) {
   cudaSetDevice(e->device);
   CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   CUDA_TRY(e, start ? cudaProfilerStart() : cudaProfilerStop());
+  return SSE_OK;
+}
+
+int sse_walker_set_T(sse_engine *e, int32_t id, double T) {
+  if (!e || !valid_id(e, id)) return SSE_ERR_ARG;
+  if (!(T > 0) || !std::isfinite(T)) return fail(e, SSE_ERR_ARG, "temperature must be positive and finite");
+  cudaSetDevice(e->device);
+  char *dst = reinterpret_cast<char *>(e->d_walkers + id) + offsetof(DevWalker, T);
+  CUDA_TRY(e, cudaMemcpyAsync(dst, &T, sizeof(double), cudaMemcpyHostToDevice, e->stream));
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  return SSE_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// checks a ladder layout: ids distinct and valid, one model per ladder
+int check_ladders(sse_engine *e, int32_t nladders, int32_t nrungs, const int32_t *ids) {
+  if (nladders < 0 || nrungs < 2 || nrungs > PT_MAX_RUNGS || (nladders && !ids))
+    return fail(e, SSE_ERR_ARG, "ladders need 2..1024 rungs");
+  std::vector<char> seen(e->walkers.size(), 0);
+  for (int l = 0; l < nladders; l++) {
+    const int32_t *lid = ids + (size_t)l * nrungs;
+    for (int k = 0; k < nrungs; k++) {
+      if (!valid_id(e, lid[k])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+      if (seen[lid[k]]) return fail(e, SSE_ERR_ARG, "a walker appears twice in the ladders");
+      seen[lid[k]] = 1;
+      if (e->walkers[lid[k]].model != e->walkers[lid[0]].model)
+        return fail(e, SSE_ERR_ARG, "the walkers of a ladder must share one model");
+    }
+  }
+  return SSE_OK;
+}
+
+struct PtBuffers {
+  int32_t *ids = nullptr, *accepted = nullptr;
+  long long *acc = nullptr, *prop = nullptr;
+  int *err = nullptr;
+  size_t npairs = 0;
+};
+
+int pt_alloc(sse_engine *e, PtBuffers &b, int32_t nladders, int32_t nrungs, const int32_t *ids) {
+  b.npairs = (size_t)nladders * (nrungs - 1);
+  int rc = dev_alloc(e, &b.ids, (size_t)nladders * nrungs);
+  if (!rc) rc = dev_alloc(e, &b.accepted, b.npairs);
+  if (!rc) rc = dev_alloc(e, &b.acc, b.npairs);
+  if (!rc) rc = dev_alloc(e, &b.prop, b.npairs);
+  if (!rc) rc = dev_alloc(e, &b.err, 1);
+  if (rc) return rc;
+  CUDA_TRY(e, cudaMemcpyAsync(b.ids, ids, sizeof(int32_t) * (size_t)nladders * nrungs, cudaMemcpyHostToDevice,
+                              e->stream));
+  CUDA_TRY(e, cudaMemsetAsync(b.acc, 0, sizeof(long long) * b.npairs, e->stream));
+  CUDA_TRY(e, cudaMemsetAsync(b.prop, 0, sizeof(long long) * b.npairs, e->stream));
+  CUDA_TRY(e, cudaMemsetAsync(b.err, 0, sizeof(int), e->stream));
+  return SSE_OK;
+}
+
+void pt_free(sse_engine *e, PtBuffers &b) {
+  dev_free(e, b.ids);
+  dev_free(e, b.accepted);
+  dev_free(e, b.acc);
+  dev_free(e, b.prop);
+  dev_free(e, b.err);
+}
+
+int pt_launch(sse_engine *e, PtBuffers &b, int32_t nladders, int32_t nrungs, uint64_t seed, uint64_t step) {
+  const int threads = std::min(256, (nrungs + 31) & ~31);
+  k_tempering<<<nladders, threads, 0, e->stream>>>(e->d_walkers, e->d_models, b.ids, nrungs, seed, step, b.accepted,
+                                                    b.acc, b.prop, b.err);
+  CUDA_TRY(e, cudaGetLastError());
+  e->last_launches += 1;
+  return SSE_OK;
+}
+
+int pt_check_err(sse_engine *e, PtBuffers &b) {
+  int err = 0;
+  CUDA_TRY(e, cudaMemcpyAsync(&err, b.err, sizeof(int), cudaMemcpyDeviceToHost, e->stream));
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  if (err) return fail(e, SSE_ERR_ARG, "the temperatures of a ladder must be distinct");
+  return SSE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sse_tempering_exchange(sse_engine *e, int32_t nladders, int32_t nrungs, const int32_t *ids, uint64_t seed,
+                           uint64_t step, int32_t *accepted) {
+  if (!e) return SSE_ERR_ARG;
+  int rc = check_ladders(e, nladders, nrungs, ids);
+  if (rc || nladders == 0) return rc;
+  cudaSetDevice(e->device);
+  e->last_launches = 0;
+  PtBuffers b;
+  rc = pt_alloc(e, b, nladders, nrungs, ids);
+  if (!rc) {
+    CUDA_TRY(e, cudaEventRecord(e->ev0, e->stream));
+    rc = pt_launch(e, b, nladders, nrungs, seed, step);
+  }
+  if (!rc) {
+    CUDA_TRY(e, cudaEventRecord(e->ev1, e->stream));
+    if (accepted)
+      CUDA_TRY(e, cudaMemcpyAsync(accepted, b.accepted, sizeof(int32_t) * b.npairs, cudaMemcpyDeviceToHost,
+                                  e->stream));
+    rc = pt_check_err(e, b);
+    float ms = 0.0f;
+    if (!rc && cudaEventElapsedTime(&ms, e->ev0, e->ev1) == cudaSuccess) e->last_ms = ms;
+  }
+  pt_free(e, b);
+  return rc;
+}
+
+int sse_sweep_tempering(sse_engine *e, int32_t nladders, int32_t nrungs, const int32_t *ids, int32_t nblocks,
+                        int32_t interval, uint64_t seed, uint64_t first_step, uint32_t flags,
+                        int64_t *accepted_counts, int64_t *proposed_counts) {
+  if (!e || nblocks < 0 || interval < 0) return SSE_ERR_ARG;
+  if (flags & SSE_SWEEP_PLAIN) return fail(e, SSE_ERR_ARG, "sse_sweep_tempering runs batched launches");
+  int rc = check_ladders(e, nladders, nrungs, ids);
+  if (rc || nladders == 0) return rc;
+  cudaSetDevice(e->device);
+  PtBuffers b;
+  rc = pt_alloc(e, b, nladders, nrungs, ids);
+  if (rc) {
+    pt_free(e, b);
+    return rc;
+  }
+  const std::vector<int32_t> work(ids, ids + (size_t)nladders * nrungs);
+  double ms = 0.0;
+  long long launches = 0;
+  int first_error = 0;
+  std::string err_msg;
+  for (int blk = 0; blk < nblocks && !rc; blk++) {
+    int r = run_until_done(e, MODE_SWEEP, work, interval, flags);
+    ms += e->last_ms;
+    launches += e->last_launches;
+    if (r == SSE_ERR_INVALID_VERTEX || r == SSE_ERR_WORM_CAP) {
+      // walker-level failure: the exchange skips pairs with a stopped walker, the rest go on
+      if (!first_error) {
+        first_error = r;
+        err_msg = e->err;
+      }
+    } else if (r) {
+      rc = r;
+      break;
+    }
+    e->last_launches = 0;
+    CUDA_TRY(e, cudaEventRecord(e->ev0, e->stream));
+    rc = pt_launch(e, b, nladders, nrungs, seed, first_step + (uint64_t)blk);
+    if (rc) break;
+    CUDA_TRY(e, cudaEventRecord(e->ev1, e->stream));
+    rc = pt_check_err(e, b);
+    float t = 0.0f;
+    if (!rc && cudaEventElapsedTime(&t, e->ev0, e->ev1) == cudaSuccess) ms += t;
+    launches += 1;
+  }
+  if (!rc && (accepted_counts || proposed_counts)) {
+    if (accepted_counts)
+      CUDA_TRY(e, cudaMemcpyAsync(accepted_counts, b.acc, sizeof(long long) * b.npairs, cudaMemcpyDeviceToHost,
+                                  e->stream));
+    if (proposed_counts)
+      CUDA_TRY(e, cudaMemcpyAsync(proposed_counts, b.prop, sizeof(long long) * b.npairs, cudaMemcpyDeviceToHost,
+                                  e->stream));
+    CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  }
+  pt_free(e, b);
+  e->last_ms = ms;
+  e->last_launches = launches;
+  if (rc) return rc;
+  if (first_error) return fail(e, first_error, err_msg);
   return SSE_OK;
 }
 

@@ -125,6 +125,10 @@ def lib():
             "sse_get_launch": ([eng, P(I32), P(I32)], C.c_int),
             "sse_profiler_range": ([eng, I32], C.c_int),
             "sse_autotune": ([eng, I32, P(I32), I32, U32, P(I32), P(C.c_double)], C.c_int),
+            "sse_walker_set_T": ([eng, I32, C.c_double], C.c_int),
+            "sse_tempering_exchange": ([eng, I32, I32, P(I32), C.c_uint64, C.c_uint64, P(I32)], C.c_int),
+            "sse_sweep_tempering": ([eng, I32, I32, P(I32), I32, I32, C.c_uint64, C.c_uint64, U32, P(I64), P(I64)],
+                                    C.c_int),
             "sse_sweep_noalloc": ([P(ModelDesc), C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p, C.c_void_p,
                                    C.c_void_p, I32, U32], C.c_int),
         }
@@ -143,7 +147,7 @@ def exported_symbols():
         "sse_model_nobs", "sse_walkers_create", "sse_walkers_destroy", "sse_walkers_reserve", "sse_walkers_init",
         "sse_sweep", "sse_sweep_each", "sse_observables", "sse_walker_info_get", "sse_walker_export", "sse_walker_import",
         "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range", "sse_autotune",
-        "sse_sweep_noalloc",
+        "sse_sweep_noalloc", "sse_walker_set_T", "sse_tempering_exchange", "sse_sweep_tempering",
     ]
 
 
@@ -342,6 +346,39 @@ class Engine:
 
     def profiler_range(self, start: bool):
         self._check(self._L.sse_profiler_range(self.h, int(bool(start))))
+
+    def set_T(self, wid: int, T: float):
+        """Carlo.parallel_tempering_change_parameter!(mc, :T, T) (src/sse.jl:399-405)."""
+        self._check(self._L.sse_walker_set_T(self.h, int(wid), float(T)))
+
+    @staticmethod
+    def _ladders(ids):
+        a = np.ascontiguousarray(ids, dtype=np.int32)
+        if a.ndim != 2 or a.shape[1] < 2:
+            raise ValueError("ladders are given as an array of shape (nladders, nrungs >= 2)")
+        return a, a.shape[0], a.shape[1]
+
+    def tempering_exchange(self, ladders, seed: int, step: int) -> np.ndarray:
+        """One parallel-tempering exchange step (sse_tempering_exchange); returns the accept flags
+        (1, 0, or -1 for pairs not proposed), shape (nladders, nrungs - 1), pairs in T order."""
+        a, nl, nr = self._ladders(ladders)
+        acc = np.zeros((nl, nr - 1), dtype=np.int32)
+        self._check(self._L.sse_tempering_exchange(self.h, nl, nr, _p(a, C.c_int32), int(seed), int(step),
+                                                   _p(acc, C.c_int32)))
+        return acc
+
+    def sweep_tempering(self, ladders, nblocks: int, interval: int, seed: int, first_step: int = 0,
+                        measure: bool = True, graph: bool = False):
+        """nblocks x (interval Carlo steps + one exchange step); returns (accepted, proposed) counts per
+        rung pair, shape (nladders, nrungs - 1)."""
+        a, nl, nr = self._ladders(ladders)
+        acc = np.zeros((nl, nr - 1), dtype=np.int64)
+        prop = np.zeros((nl, nr - 1), dtype=np.int64)
+        flags = (SSE_SWEEP_MEASURE if measure else 0) | (SSE_SWEEP_GRAPH if graph else 0)
+        self._check(self._L.sse_sweep_tempering(self.h, nl, nr, _p(a, C.c_int32), int(nblocks), int(interval),
+                                                int(seed), int(first_step), flags, _p(acc, C.c_int64),
+                                                _p(prop, C.c_int64)))
+        return acc, prop
 
     def set_launch(self, warps_per_block: int = 0, blocks_per_sm: int = 0):
         """Warps (walkers) per block of the batched kernel (1..4; 0 = automatic) and a cap on blocks per SM."""

@@ -8,10 +8,12 @@ Reference interface (src/sse.jl):
     Carlo.measure!(mc, ctx)          src/sse.jl:70-87
     Carlo.write_checkpoint / read_checkpoint   src/sse.jl:89-107
     Carlo.register_evaluables        src/sse.jl:111-134, magnetization_estimator.jl:236-258
+    Carlo.parallel_tempering_log_weight_ratio / _change_parameter!   src/sse.jl:390-405
 
 ``MC`` drives one walker; ``BatchMC`` drives many walkers of one parameter set
 in a single persistent launch per sweep block, which is how the engine is
-meant to be used.  Both go through ``engine.Engine`` (the C ABI) and raise if
+meant to be used; ``TemperingMC`` runs ladders of walkers over a temperature
+list with exchange steps on the device.  Both go through ``engine.Engine`` (the C ABI) and raise if
 the CUDA library is missing -- there is no CPU fallback.
 
 Parameter names follow the reference: ``T``, ``model`` (a model class such as
@@ -22,6 +24,8 @@ Parameter names follow the reference: ``T``, ``model`` (a model class such as
 """
 
 from __future__ import annotations
+
+import math
 
 import numpy as np
 
@@ -82,10 +86,24 @@ class MC:
         self.model_id = self.engine.register_model(self.flat)
         self.wid = int(self.engine.create_walkers(self.model_id, [_walker_params(params, stream)])[0])
         self.names = observable_names(self.flat.est_prefixes)
+        self._T = float(params["T"])
 
     @property
     def T(self) -> float:
-        return float(self.params["T"])
+        return self._T
+
+    # ---- parallel tempering hooks (src/sse.jl:390-405) ----
+    def parallel_tempering_log_weight_ratio(self, parameter: str, new_value: float) -> float:
+        if parameter != "T":
+            raise ValueError(f"unsupported parallel tempering parameter {parameter}")
+        n = self.engine.info(self.wid)["num_operators"]
+        return -n * math.log(new_value / self._T)
+
+    def parallel_tempering_change_parameter(self, parameter: str, new_value: float):
+        if parameter != "T":
+            raise ValueError(f"unsupported parallel tempering parameter {parameter}")
+        self.engine.set_T(self.wid, float(new_value))
+        self._T = float(new_value)
 
     # ---- Carlo.AbstractMC ----
     def init(self, ctx: MCContext, params: dict | None = None):
@@ -182,17 +200,108 @@ class BatchMC:
 
     def results(self) -> dict:
         """Evaluables with jackknife errors over all bins of all walkers: name -> (mean, error)."""
-        keys = [k for k in self.names if not all(np.isnan(b[k]) for b in self.bins)]
-        arr = {k: np.array([b[k] for b in self.bins]) for k in keys}
-        nb = len(self.bins)
-        tot = {k: np.nansum(v) for k, v in arr.items()}
-        full = evaluables({k: tot[k] / nb for k in keys}, self.flat.est_prefixes, self.flat.norm_site_count)
-        loo = [evaluables({k: (tot[k] - arr[k][i]) / (nb - 1) for k in keys}, self.flat.est_prefixes,
-                          self.flat.norm_site_count) for i in range(nb)]
-        res = {}
-        for name, v in full.items():
-            x = np.array([l[name] for l in loo])
-            res[name] = (v, float(np.sqrt((nb - 1) / nb * np.sum((x - x.mean()) ** 2))))
-        for k in keys:
-            res.setdefault(k, (float(np.nanmean(arr[k])), float(np.nanstd(arr[k]) / np.sqrt(max(nb, 1)))))
-        return res
+        return jackknife_results(self.bins, self.names, self.flat)
+
+
+def jackknife_results(bins: list, names: list, flat) -> dict:
+    """Evaluables with jackknife errors over bins (dicts of observable means): name -> (mean, error)."""
+    keys = [k for k in names if not all(np.isnan(b[k]) for b in bins)]
+    arr = {k: np.array([b[k] for b in bins]) for k in keys}
+    nb = len(bins)
+    tot = {k: np.nansum(v) for k, v in arr.items()}
+    full = evaluables({k: tot[k] / nb for k in keys}, flat.est_prefixes, flat.norm_site_count)
+    loo = [evaluables({k: (tot[k] - arr[k][i]) / (nb - 1) for k in keys}, flat.est_prefixes, flat.norm_site_count)
+           for i in range(nb)]
+    res = {}
+    for name, v in full.items():
+        x = np.array([l[name] for l in loo])
+        res[name] = (v, float(np.sqrt((nb - 1) / nb * np.sum((x - x.mean()) ** 2))))
+    for k in keys:
+        res.setdefault(k, (float(np.nanmean(arr[k])), float(np.nanstd(arr[k]) / np.sqrt(max(nb, 1)))))
+    return res
+
+
+class TemperingMC:
+    """Parallel tempering in T (src/sse.jl:390-405) over resident walkers.
+
+    ``nladders`` independent ladders, each holding one walker per entry of ``temperatures`` (walker
+    (l, k) starts at temperatures[k] with stream first_stream + l*len(temperatures) + k).  Every
+    ``interval`` Carlo steps the device runs one exchange step: the walkers of a ladder, ranked by
+    T, propose the rung pairs (k, k+1) with k of alternating parity and swap temperatures with the
+    Metropolis weight built from parallel_tempering_log_weight_ratio.  The observable accumulators
+    move with the temperature, so every bin is per temperature.
+    """
+
+    def __init__(self, params: dict, temperatures, nladders: int = 1, interval: int = 10,
+                 engine: Engine | None = None, first_stream: int = 0, exchange_seed: int | None = None):
+        temps = [float(t) for t in temperatures]
+        if len(temps) < 2 or len(set(temps)) != len(temps):
+            raise ValueError("a ladder needs at least two distinct temperatures")
+        self.params = params
+        self.temperatures = temps
+        self.interval = int(interval)
+        self.model = params["model"](params)
+        self.flat = flatten_model(self.model)
+        self.engine = engine or default_engine(int(params.get("device", 0)))
+        self.model_id = self.engine.register_model(self.flat)
+        nr = len(temps)
+        wp = []
+        for l in range(nladders):
+            for k in range(nr):
+                p = _walker_params(dict(params, T=temps[k]), first_stream + l * nr + k)
+                wp.append(p)
+        self.ladders = self.engine.create_walkers(self.model_id, wp).reshape(nladders, nr)
+        self.names = observable_names(self.flat.est_prefixes)
+        self.seed = int(params.get("seed", 0)) if exchange_seed is None else int(exchange_seed)
+        self.step = 0
+        self.accepted = np.zeros((nladders, nr - 1), dtype=np.int64)
+        self.proposed = np.zeros((nladders, nr - 1), dtype=np.int64)
+        self.bins: list = [[] for _ in temps]
+
+    def init(self):
+        self.engine.init(self.ladders.ravel())
+
+    def sweep(self, nblocks: int, measure: bool = True):
+        """nblocks x (interval Carlo steps of every walker + one exchange step)."""
+        acc, prop = self.engine.sweep_tempering(self.ladders, nblocks, self.interval, self.seed, self.step,
+                                                measure=measure)
+        self.step += nblocks
+        self.accepted += acc
+        self.proposed += prop
+
+    def temperature_of(self) -> np.ndarray:
+        """Current temperature index of every walker, shape (nladders, nrungs)."""
+        idx = {t: k for k, t in enumerate(self.temperatures)}
+        return np.array([[idx[self.engine.info(int(w))["T"]] for w in row] for row in self.ladders])
+
+    def collect_bin(self):
+        """One bin per (ladder, temperature) from the accumulators, which hold the measurements taken at
+        the walker's current temperature."""
+        where = self.temperature_of()
+        for l, row in enumerate(self.ladders):
+            out = self.engine.observables(row, reset=True)
+            for k, (s, c, _) in enumerate(out):
+                self.bins[where[l, k]].append(
+                    {n: (s[i] / c[i] if c[i] else np.nan) for i, n in enumerate(self.names)})
+
+    def run(self, sweeps: int, binsize: int):
+        """init!, thermalisation (with exchanges), then measured sweeps in bins of `binsize` (rounded up
+        to whole exchange intervals)."""
+        therm = int(self.params.get("thermalization", 0))
+        blocks_per_bin = max(1, -(-int(binsize) // self.interval))
+        self.init()
+        self.sweep(-(-therm // self.interval) if therm else 0)
+        for row in self.ladders:
+            self.engine.observables(row, reset=True)
+        for _ in range(max(1, sweeps // (blocks_per_bin * self.interval))):
+            self.sweep(blocks_per_bin)
+            self.collect_bin()
+
+    def acceptance(self) -> np.ndarray:
+        """Accepted / proposed swaps per rung pair, summed over ladders."""
+        p = self.proposed.sum(0)
+        return np.where(p > 0, self.accepted.sum(0) / np.maximum(p, 1), np.nan)
+
+    def results(self) -> list:
+        """Per temperature: evaluables with jackknife errors, name -> (mean, error)."""
+        return [jackknife_results(b, self.names, self.flat) for b in self.bins]
