@@ -56,9 +56,11 @@ def parse():
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--profile", action="store_true", help="open a profiler range around the timed steps only")
     ap.add_argument("--serving-requests", type=int, default=200, help="requests in the serving run (0: skip)")
-    ap.add_argument("--workload", default="uniform", choices=["uniform", "single", "uneven", "bilayer"],
+    ap.add_argument("--workload", default="uniform",
+                    choices=["uniform", "single", "uneven", "bilayer", "magnet_bench", "cluster_bench"],
                     help="uniform: the headline batch; single: one 8x8 walker at beta=2; uneven: 8192 walkers of "
-                         "mixed sizes and temperatures; bilayer: 2048 S=1 bilayer walkers 48x48")
+                         "mixed sizes and temperatures; bilayer: 2048 S=1 bilayer walkers 48x48; magnet_bench / "
+                         "cluster_bench: the reference's own whole-job benchmark tasks, batched")
     return ap.parse_args()
 
 
@@ -367,8 +369,90 @@ def run_other_workload(args):
                     sweeps_per_step=args.sweeps_per_step, steps=args.steps, walker_sweeps_per_s=ws / t_dev,
                     operator_updates_per_s=ou / t_dev, walkers_stopped_by_worm_cap=failed,
                     cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
+    elif args.workload in ("magnet_bench", "cluster_bench"):
+        line.update(run_reference_job(S, eng, args))
     eng.close()
     print(json.dumps(line), flush=True)
+
+
+def reference_job_model(S, name):
+    """The benchmark tasks of the reference's test/test_jobs.jl:113-165, timed there by
+    test/benchmarks.jl:20-40 (one task: 2000 thermalisation + 5000 measured sweeps)."""
+    if name == "magnet_bench":
+        p = {"lattice": {"unitcell": S.UnitCells.square, "size": (10, 10)}, "J": 1.23, "hz": -0.2,
+             "measure": S.all_magnetization_estimators(2)}
+        return S.MagnetModel(p), 0.05, "10x10 square S=1/2, J=1.23, hz=-0.2, T=0.05, all magnetization estimators"
+    p = {"inner_model": S.MagnetModel, "lattice": {"unitcell": S.UnitCells.fully_frust_square_bilayer, "size": (30, 30)},
+         "parameter_map": {"S": ["Sa", "Sb"], "J": ["JD"] + ["JP"] * 8}, "cluster_bases": (S.ClusterBases.dimer,),
+         "measure_quantum_numbers": [{"name": "", "quantum_number": 2}], "JD": 0.5, "JP": 1.0, "Sa": 0.5, "Sb": 0.5}
+    return (S.ClusterModel(p), 0.1,
+            "30x30 fully frustrated square bilayer in the dimer basis (900 dims-4 sites), JD=0.5, JP=1, T=0.1")
+
+
+def run_reference_job(S, eng, args):
+    """One of the reference's benchmark tasks: `--walkers` independent copies batched on the GPU, a single
+    copy on the GPU, and the CPU oracle (one chain per core, and one chain on one core)."""
+    from oracle import oracle as O
+
+    model, T, desc = reference_job_model(S, args.workload)
+    flat = S.flatten_model(model)
+    mid = eng.register_model(flat)
+    # the reference's task is 2000 + 5000 sweeps; --therm and --steps x --sweeps-per-step set the sample
+    therm, sweeps = args.therm, args.steps * args.sweeps_per_step
+    nw = args.walkers
+    ids = eng.create_walkers(mid, [dict(T=T, seed=args.seed, stream=k, thermalization=therm) for k in range(nw)])
+    eng.init(ids)
+    t0 = time.perf_counter()
+    ids, failed = sweep_tolerant(eng, ids, therm, measure=True)
+    therm_dev = eng.last_timing()[0] / 1e3
+    info0 = {i: eng.info(i) for i in ids.tolist()}
+    ids, f = sweep_tolerant(eng, ids, sweeps, measure=True)
+    failed += f
+    meas_dev = eng.last_timing()[0] / 1e3
+    wall = time.perf_counter() - t0
+    info1 = {i: eng.info(i) for i in ids.tolist()}
+    ou = sum(info1[i]["slot_visits"] + info1[i]["worm_steps"] - info0[i]["slot_visits"] - info0[i]["worm_steps"]
+             for i in ids.tolist())
+    # one copy alone on the GPU (latency-bound), a short sample
+    (one,) = eng.create_walkers(mid, [dict(T=T, seed=args.seed, stream=nw + 1, thermalization=therm)])
+    eng.init([one])
+    n_single = max(1, min(200, sweeps // 10))
+    eng.sweep([one], n_single, measure=True)
+    eng.sweep([one], n_single, measure=True)
+    single_s = eng.last_timing()[0] / 1e3
+    # the CPU oracle: a bounded sample from a GPU-thermalised state
+    om = O.OracleModel(flat)
+    nthreads = args.cpu_threads or os.cpu_count() or 1
+    chains = []
+    for k, wid in enumerate(ids.tolist()[:nthreads]):
+        ops, st, inf = eng.export(wid)
+        w = O.OracleWalker(om, T=T, seed=args.seed, stream=k, thermalization=0)
+        w.set_opstring(ops, inf["num_operators"])
+        w.set_state(st)
+        w.w.num_worms = inf["num_worms"]
+        w.w.avg_worm_length = inf["avg_worm_length"]
+        w.w.ctr = inf["rng_counter"]
+        chains.append(w)
+    cpu_sweeps = max(1, args.cpu_sweeps)
+    t0 = time.perf_counter()
+    chains[0].run(cpu_sweeps, measure=True)
+    cpu_one = cpu_sweeps / (time.perf_counter() - t0)
+    t0 = time.perf_counter()
+    O.run_parallel(om, chains, cpu_sweeps, measure=True, nthreads=nthreads)
+    cpu_all = len(chains) * cpu_sweeps / (time.perf_counter() - t0)
+    Ls = np.array([info1[i]["L"] for i in ids.tolist()])
+    return dict(
+        config=desc, reference_task="2000 thermalisation + 5000 measured sweeps per walker",
+        thermalization_sweeps=therm, measured_sweeps=sweeps, cpu_sample_sweeps=cpu_sweeps,
+        walkers=nw, walkers_stopped_by_worm_cap=failed,
+        gpu_batched_walker_sweeps_per_s=len(ids) * sweeps / meas_dev,
+        gpu_batched_operator_updates_per_s=ou / meas_dev,
+        gpu_batched_job_seconds_device=therm_dev + meas_dev, gpu_batched_job_seconds_wall=wall,
+        gpu_single_walker_sweeps_per_s=n_single / single_s,
+        cpu_oracle_one_core_sweeps_per_s=cpu_one,
+        cpu_oracle_all_cores_walker_sweeps_per_s=cpu_all, cpu_threads=nthreads,
+        cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())],
+    )
 
 
 def main():

@@ -17,5 +17,6 @@ from .magnet import (
     magnetization_estimator_standard_prefix,
 )
 from .tables import FlatModel, flatten_model, flatten_sse_data
+from .cluster import ClusterBasis, ClusterBases, ClusterModel, lift_twobody_operator, build_cluster_hamiltonians
 from . import engine
 from .mc import MC, MCContext, BatchMC, TemperingMC

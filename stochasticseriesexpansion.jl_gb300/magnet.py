@@ -39,6 +39,7 @@ class MagnetizationEstimatorSpec:
     ordering_vector: tuple
     stagger_uc: bool
     prefix: str
+    tag: int | None = None  # quantum-number index for cluster models (cluster.jl:226-239)
 
 
 def magnetization_estimator_standard_prefix(q, stagger_uc: bool) -> str:
@@ -144,7 +145,7 @@ class MagnetModel(AbstractModel):
             dims, H, factor = generate_bond_hamiltonian(
                 bp, (self.site_spin_states[uc_bond.iuc - 1], self.site_spin_states[uc_bond.juc - 1])
             )
-            vds.append(make_vertex_data(dims, H, energy_offset_factor=factor))
+            vds.append(make_vertex_data(dims, H, energy_offset_factor=factor, lp_point=self.params.get("lp_point")))
         bonds = [SSEBond(b.type, (b.i, b.j)) for b in self.lattice.bonds]
         return SSEData.make(vds, bonds)
 

@@ -133,9 +133,16 @@ def flatten_sse_data(sse_data, estimators=(), model=None, norm_site_count=None) 
     est_coef = np.zeros(len(ests) * N * maxdim, dtype=np.float64)
     for e, spec in enumerate(ests):
         for site in range(1, N + 1):
-            sg = model.lattice.staggered_sign(spec.ordering_vector, spec.stagger_uc, site)
+            if hasattr(model, "staggered_sign"):
+                sg = model.staggered_sign(spec, site)
+            else:
+                sg = model.lattice.staggered_sign(spec.ordering_vector, spec.stagger_uc, site)
             for s in range(site_dims[site - 1]):
-                est_coef[(e * N + site - 1) * maxdim + s] = sg * model.magnetization_state(site, s + 1)
+                if spec.tag is None:
+                    m = model.magnetization_state(site, s + 1)
+                else:
+                    m = model.magnetization_state(site, s + 1, spec.tag)
+                est_coef[(e * N + site - 1) * maxdim + s] = sg * m
 
     if norm_site_count is None:
         norm_site_count = model.normalization_site_count() if model is not None else N

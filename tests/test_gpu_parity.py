@@ -39,13 +39,26 @@ def bilayer_s1(S, L=4):
                           "measure": ["magnetization"]})
 
 
+def cluster_dimer(S):
+    """The reference's cluster ED job (test/test_jobs.jl:70-104): dims-4 dimer sites, signed tables."""
+    return S.ClusterModel({
+        "inner_model": S.MagnetModel,
+        "lattice": {"unitcell": S.UnitCells.fully_frust_square_bilayer, "size": (3, 2)},
+        "parameter_map": {"S": ["Sa", "Sb"], "J": ["JD", "JxP", "JxP", "JyP", "JyP", "JxX", "JxX", "JyX", "JyX"]},
+        "cluster_bases": (S.ClusterBases.dimer,),
+        "measure_quantum_numbers": [{"name": "", "quantum_number": 2}],
+        "JD": 1, "JxP": 0.55, "JyP": 0.6, "JxX": 0.7, "JyX": 0.3, "d": -0.2, "Dz": 0.2, "Dx": 0.5,
+        "Sa": 0.5, "Sb": 0.5})
+
+
 _FLAT = {}
 
 
 def flat_of(S, name):
     if name not in _FLAT:
         m = {"sq8": lambda: sq_model(S), "honey": lambda: honeycomb_mixed(S), "bilayer": lambda: bilayer_s1(S),
-             "sq32": lambda: sq_model(S, 32), "sq4": lambda: sq_model(S, 4)}[name]()
+             "sq32": lambda: sq_model(S, 32), "sq4": lambda: sq_model(S, 4),
+             "cluster": lambda: cluster_dimer(S)}[name]()
         _FLAT[name] = S.flatten_model(m)
     return _FLAT[name]
 
@@ -85,7 +98,8 @@ def test_gpu_vertex_list_golden(S, eng):
     assert np.array_equal(vl, evl)
 
 
-@pytest.mark.parametrize("name,T", [("sq8", 0.5), ("honey", 0.1), ("bilayer", 0.25), ("sq4", 4.0)])
+@pytest.mark.parametrize("name,T", [("sq8", 0.5), ("honey", 0.1), ("bilayer", 0.25), ("sq4", 4.0), ("cluster", 0.3),
+                                    ("cluster", 0.05)])
 def test_gpu_init_and_sweeps_match_oracle(S, O, eng, name, T):
     flat = flat_of(S, name)
     mid = eng.register_model(flat)
