@@ -148,6 +148,12 @@ def dist_setup(args):
     return rank, world, local
 
 
+def replica_streams(rank, nwalkers):
+    """Walker ids (Philox streams) of one replica: rank r runs streams r*n .. r*n + n - 1, so the
+    replicas of a multi-GPU run are disjoint sets of independent chains (no data exchange)."""
+    return range(rank * nwalkers, (rank + 1) * nwalkers)
+
+
 def barrier_max(world, x):
     if world == 1:
         return x
@@ -472,8 +478,8 @@ def main():
     eng = Engine(local)
     mid = eng.register_model(flat)
     nw = args.walkers
-    ids = eng.create_walkers(mid, [dict(T=1.0 / args.beta, seed=args.seed, stream=rank * nw + k,
-                                        thermalization=args.therm) for k in range(nw)])
+    ids = eng.create_walkers(mid, [dict(T=1.0 / args.beta, seed=args.seed, stream=st, thermalization=args.therm)
+                                   for st in replica_streams(rank, nw)])
     eng.init(ids)
     # thermalisation (controller active), in blocks
     done = 0
