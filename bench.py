@@ -312,8 +312,18 @@ def run_other_workload(args):
         eng.init([a, b])
         eng.sweep([a, b], 2000, measure=False)
         n = 20000
+        c0 = np.array(eng.info(int(a))["phase_cycles"], dtype=float)
         eng.sweep([a], n, measure=True)
         ms, _ = eng.last_timing()
+        c1 = np.array(eng.info(int(a))["phase_cycles"], dtype=float)
+        # the same walker with its records staged in shared memory for the worm update
+        eng.set_staging(192 * 1024)
+        eng.sweep([a], n, measure=True)
+        ms_staged, _ = eng.last_timing()
+        c2 = np.array(eng.info(int(a))["phase_cycles"], dtype=float)
+        eng.set_staging(0)
+        line.update(cycles_per_sweep_diag_link_worm_measure=[round(x) for x in (c1 - c0) / n],
+                    staged_cycles_per_sweep_diag_link_worm_measure=[round(x) for x in (c2 - c1) / n])
         t0 = time.perf_counter()
         eng.sweep([b], 500, measure=True, plain=True)
         plain_s = time.perf_counter() - t0
@@ -327,6 +337,7 @@ def run_other_workload(args):
         w.run(n, measure=True)
         cpu_s = time.perf_counter() - t0
         line.update(config="8x8 S=1/2 Heisenberg, beta=2, one walker", gpu_persistent_sweeps_per_s=n / (ms / 1e3),
+                    gpu_persistent_staged_sweeps_per_s=n / (ms_staged / 1e3),
                     gpu_plain_sweeps_per_s=500 / plain_s, cpu_oracle_one_core_sweeps_per_s=n / cpu_s,
                     mean_L=eng.info(int(a))["L"])
     elif args.workload in ("uneven", "bilayer"):

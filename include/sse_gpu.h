@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define SSE_GPU_ABI_VERSION 1
+#define SSE_GPU_ABI_VERSION 2
 
 typedef enum sse_status {
   SSE_OK = 0,
@@ -178,11 +178,19 @@ int sse_last_timing(sse_engine *eng, double *ms, int64_t *launches);
 /* launch shape of the batched kernel: warps (walkers) per block, 1..4; 0 = automatic (4) */
 int sse_set_launch(sse_engine *eng, int32_t warps_per_block, int32_t blocks_per_sm);
 int sse_get_launch(sse_engine *eng, int32_t *warps_per_block, int32_t *blocks_per_sm);
-/* times nsweeps_probe sweeps of the given walkers with 1, 2 and 4 walkers per block and keeps the
- * fastest launch shape; the probe sweeps are ordinary Carlo steps of those walkers (run it during
+/* shared-memory staging: a walker whose compacted operator records (32 bytes per non-identity
+ * operator) fit in stage_bytes runs its worm update on a copy in shared memory instead of chasing
+ * links through HBM; 0 (default) turns it off.  Every warp of the sweep kernel then holds
+ * stage_bytes of shared memory, which lowers the number of resident walkers. */
+#define SSE_MAX_STAGE_BYTES (192 * 1024)
+int sse_set_staging(sse_engine *eng, int32_t stage_bytes);
+int sse_get_staging(sse_engine *eng, int32_t *stage_bytes);
+/* times nsweeps_probe sweeps of the given walkers for each launch shape (1, 2, 4 walkers per block)
+ * and staging budget (off, and room for the median, 90th-percentile and largest walker's records)
+ * and keeps the fastest; the probe sweeps are ordinary Carlo steps of those walkers (run it during
  * thermalisation) */
 int sse_autotune(sse_engine *eng, int32_t count, const int32_t *ids, int32_t nsweeps_probe, uint32_t flags,
-                 int32_t *best_warps_per_block, double *best_ms);
+                 int32_t *best_warps_per_block, int32_t *best_stage_bytes, double *best_ms);
 /* brackets a profiled region (cudaProfilerStart / cudaProfilerStop) for profilers started with
  * collection off; start != 0 opens the region, 0 closes it */
 int sse_profiler_range(sse_engine *eng, int32_t start);

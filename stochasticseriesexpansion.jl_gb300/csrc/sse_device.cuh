@@ -650,6 +650,9 @@ struct Chase {
 // one transition row from L1; when a record arrives its four neighbours are prefetched
 // into L1 so that the next record is in flight while the scatter resolves.  Returns with
 // `done` set when the worm closes, or with pos == DRAW_BUF when the buffer is empty.
+//
+// PF false: the records are staged in shared memory and nothing is prefetched.
+template <bool PF>
 __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long long *dbuf, int &pos,
                                           uint32_t *__restrict__ ops, Rec *__restrict__ rec, int k0, int l0, int wf0,
                                           long long cap, Chase &cs, bool &done) {
@@ -663,10 +666,12 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
   while (pos < 64) {
     const unsigned long long u53 = dbuf[pos];
     pos++;
-    prefetch_l1(rq + 2 * (ra.x >> 2));
-    prefetch_l1(rq + 2 * (ra.y >> 2));
-    prefetch_l1(rq + 2 * (ra.z >> 2));
-    prefetch_l1(rq + 2 * (ra.w >> 2));
+    if (PF) {
+      prefetch_l1(rq + 2 * (ra.x >> 2));
+      prefetch_l1(rq + 2 * (ra.y >> 2));
+      prefetch_l1(rq + 2 * (ra.z >> 2));
+      prefetch_l1(rq + 2 * (ra.w >> 2));
+    }
     const uint32_t op = (uint32_t)rb.x;
     const int vc = (int)((op >> 1) & 0x3FFu);
     const int ti = rb.z + ((vc >> 1) * 4 + leg_in) * (rb.w & 0xFF) + (wf - 1);
@@ -729,7 +734,7 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
                                         Rec *__restrict__ rec, const int32_t *__restrict__ cidx,
                                         const int32_t *__restrict__ vfirst, uint8_t *__restrict__ state,
                                         unsigned long long *dbuf, bool thermalized, double &wlf, bool &have_wlf,
-                                        long long &steps, int lane) {
+                                        long long &steps, int lane, bool pf) {
   double total = 1.0;
   const double ceil_nw = ceil(wc.num_worms);
   const long long nworms = (long long)ceil_nw;
@@ -784,7 +789,10 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
       dbuf[2 * lane + 1] = (((unsigned long long)x.w << 32) | x.z) >> 11;
       __syncwarp();
       int pos = (int)(ctr - b);
-      if (lane == 0) status = worm_steps(M, dbuf, pos, ops, rec, k0, l0, wf0, cap, cs, done);
+      if (lane == 0) {
+        if (pf) status = worm_steps<true>(M, dbuf, pos, ops, rec, k0, l0, wf0, cap, cs, done);
+        else status = worm_steps<false>(M, dbuf, pos, ops, rec, k0, l0, wf0, cap, cs, done);
+      }
       __syncwarp();
       status = __shfl_sync(FULL, status, 0);
       done = __shfl_sync(FULL, (int)done, 0) != 0;

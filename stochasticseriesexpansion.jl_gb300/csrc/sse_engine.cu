@@ -34,9 +34,11 @@ namespace {
 constexpr int MODE_INIT = 0;
 constexpr int MODE_SWEEP = 1;
 
+// smem: this warp's shared memory; its last stage_bytes (a multiple of 32) may hold the walker's
+// compacted records for the worm update when they fit
 template <int MODE>
-__device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, uint32_t flags, long long add_sweeps,
-                               int *flag_counts, int lane) {
+__device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, int smem_per_warp, int stage_bytes,
+                               uint32_t flags, long long add_sweeps, int *flag_counts, int lane) {
   Chain c;
   c.L = W->L;
   c.n = W->n;
@@ -108,13 +110,23 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, u
         slot_visits += c.L;
         __syncwarp();
         long long t1 = clock64();
-        build_links(M, c.L, ops, W->rec, W->cidx, W->vfirst, vlast, lane);
+        const long long nrec = build_links(M, c.L, ops, W->rec, W->cidx, W->vfirst, vlast, lane);
+        // records that fit the staging budget move to shared memory for the pointer chase
+        Rec *wrec = W->rec;
+        const bool staged = nrec * (long long)sizeof(Rec) <= (long long)stage_bytes;
+        if (staged) {
+          int4 *dst = reinterpret_cast<int4 *>(smem + (smem_per_warp - stage_bytes));
+          const int4 *src = reinterpret_cast<const int4 *>(W->rec);
+          for (long long i = lane; i < 2 * nrec; i += 32) dst[i] = src[i];
+          __syncwarp();
+          wrec = reinterpret_cast<Rec *>(dst);
+        }
         long long t2 = clock64();
         double wlf = 0.0;
         bool have_wlf = false;
-        status = worm_update(M, c, wc, ops, W->rec, W->cidx, W->vfirst, state,
+        status = worm_update(M, c, wc, ops, wrec, W->cidx, W->vfirst, state,
                              reinterpret_cast<unsigned long long *>(smem), thermalized, wlf, have_wlf, worm_steps,
-                             lane);
+                             lane, !staged);
         if (status != ST_OK) break;
         if (have_wlf && lane == 0) observe(W, 5, wlf);
         sweeps++;
@@ -162,13 +174,14 @@ template <int MODE>
 __global__ void __launch_bounds__(128, 7) k_walk(const DevModel *__restrict__ models, DevWalker *__restrict__ walkers,
                                               const int32_t *__restrict__ work, int nwork, int single_id, int *queue,
                                               uint32_t flags, long long add_sweeps, int smem_per_warp,
-                                              int *flag_counts) {
-  extern __shared__ __align__(16) uint8_t smem[];
+                                              int stage_bytes, int *flag_counts) {
+  extern __shared__ __align__(32) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   uint8_t *mine = smem + (size_t)(threadIdx.x >> 5) * smem_per_warp;
   if (single_id >= 0) {
     DevWalker *W = walkers + single_id;
-    process_walker<MODE>(models[W->model], W, mine, flags, add_sweeps, flag_counts, lane);
+    process_walker<MODE>(models[W->model], W, mine, smem_per_warp, stage_bytes, flags, add_sweeps, flag_counts,
+                         lane);
     return;
   }
   for (;;) {
@@ -177,7 +190,8 @@ __global__ void __launch_bounds__(128, 7) k_walk(const DevModel *__restrict__ mo
     idx = __shfl_sync(FULL, idx, 0);
     if (idx >= nwork) break;
     DevWalker *W = walkers + work[idx];
-    process_walker<MODE>(models[W->model], W, mine, flags, add_sweeps, flag_counts, lane);
+    process_walker<MODE>(models[W->model], W, mine, smem_per_warp, stage_bytes, flags, add_sweeps, flag_counts,
+                         lane);
   }
 }
 
@@ -212,7 +226,7 @@ __global__ void k_apply_growth(DevWalker *walkers, const GrowEntry *g, int n) {
 }
 
 __global__ void k_link_debug(const DevModel *models, DevWalker *walkers, int id, int32_t *vlast_out) {
-  extern __shared__ __align__(16) uint8_t smem[];
+  extern __shared__ __align__(32) uint8_t smem[];
   const int lane = threadIdx.x & 31;
   DevWalker *W = walkers + id;
   const DevModel &M = models[W->model];
@@ -391,6 +405,7 @@ struct sse_engine {
   double last_ms = 0.0;
   long long last_launches = 0;
   int warps_per_block = 0, blocks_per_sm = 0;
+  int stage_bytes = 0;  // shared-memory staging budget per walker for the worm update (0: off)
   struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
     int32_t *d_work = nullptr;
@@ -512,9 +527,12 @@ int grow_walker(sse_engine *e, int32_t id, long long need) {
   return write_walker(e, id, w);
 }
 
-int choose_launch(sse_engine *e, int max_nsites, int nwork, int &wpb, int &grid, int &smem_per_warp, bool init) {
-  // per warp: spin state (N bytes, diagonal update), per-site link tails (4N, linking), 64 draws (512 B, worms)
-  smem_per_warp = ((std::max(4 * std::max(max_nsites, 1), 512)) + 15) & ~15;
+int choose_launch(sse_engine *e, int max_nsites, int nwork, int &wpb, int &grid, int &smem_per_warp, int &stage,
+                  bool init) {
+  // per warp: spin state (N bytes, diagonal update), per-site link tails (4N, linking), 64 draws (512 B, worms),
+  // then the staging area for the records of small walkers (sweeps only)
+  stage = init ? 0 : ((e->stage_bytes + 31) & ~31);
+  smem_per_warp = (((std::max(4 * std::max(max_nsites, 1), 512)) + 31) & ~31) + stage;
   wpb = e->warps_per_block > 0 ? e->warps_per_block : 4;
   if (wpb > 4) wpb = 4;  // k_walk is compiled for at most 128 threads per block
   while (wpb > 1 && (size_t)wpb * smem_per_warp > 200 * 1024) wpb >>= 1;
@@ -535,8 +553,8 @@ int choose_launch(sse_engine *e, int max_nsites, int nwork, int &wpb, int &grid,
 // Launch one pass: persistent over d_work[0..nwork) when single_id < 0, else one warp on single_id.
 int launch_pass(sse_engine *e, int mode, int nwork, int single_id, uint32_t flags, long long add_sweeps,
                 int max_nsites) {
-  int wpb, grid, spw;
-  int rc = choose_launch(e, max_nsites, nwork, wpb, grid, spw, mode == MODE_INIT);
+  int wpb, grid, spw, stage;
+  int rc = choose_launch(e, max_nsites, nwork, wpb, grid, spw, stage, mode == MODE_INIT);
   if (rc) return rc;
   if (single_id >= 0) {
     grid = 1;
@@ -546,10 +564,10 @@ int launch_pass(sse_engine *e, int mode, int nwork, int single_id, uint32_t flag
   }
   if (mode == MODE_INIT)
     k_walk<MODE_INIT><<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(
-        e->d_models, e->d_walkers, e->d_work, nwork, single_id, e->d_queue, flags, add_sweeps, spw, e->d_flags);
+        e->d_models, e->d_walkers, e->d_work, nwork, single_id, e->d_queue, flags, add_sweeps, spw, stage, e->d_flags);
   else
     k_walk<MODE_SWEEP><<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(
-        e->d_models, e->d_walkers, e->d_work, nwork, single_id, e->d_queue, flags, add_sweeps, spw, e->d_flags);
+        e->d_models, e->d_walkers, e->d_work, nwork, single_id, e->d_queue, flags, add_sweeps, spw, stage, e->d_flags);
   CUDA_TRY(e, cudaGetLastError());
   e->last_launches += 1;
   return SSE_OK;
@@ -596,15 +614,15 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
         CUDA_TRY(e, cudaMemcpyAsync(g.d_work, work.data(), sizeof(int32_t) * work.size(), cudaMemcpyHostToDevice,
                                     e->stream));
         CUDA_TRY(e, cudaStreamSynchronize(e->stream));
-        int wpb, grid, spw;
-        rc = choose_launch(e, max_ns, n, wpb, grid, spw, false);
+        int wpb, grid, spw, stage;
+        rc = choose_launch(e, max_ns, n, wpb, grid, spw, stage, false);
         if (rc) return rc;
         cudaGraph_t graph;
         CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
         cudaMemsetAsync(e->d_flags, 0, 2 * sizeof(int), e->stream);
         cudaMemsetAsync(e->d_queue, 0, sizeof(int), e->stream);
         k_walk<MODE_SWEEP><<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(
-            e->d_models, e->d_walkers, g.d_work, n, -1, e->d_queue, flags, add, spw, e->d_flags);
+            e->d_models, e->d_walkers, g.d_work, n, -1, e->d_queue, flags, add, spw, stage, e->d_flags);
         CUDA_TRY(e, cudaStreamEndCapture(e->stream, &graph));
         CUDA_TRY(e, cudaGraphInstantiate(&g.exec, graph, 0));
         cudaGraphDestroy(graph);
@@ -1287,25 +1305,68 @@ int sse_set_launch(sse_engine *e, int32_t warps_per_block, int32_t blocks_per_sm
   return SSE_OK;
 }
 
+int sse_set_staging(sse_engine *e, int32_t stage_bytes) {
+  if (!e || stage_bytes < 0 || stage_bytes > SSE_MAX_STAGE_BYTES) return SSE_ERR_ARG;
+  const int rounded = (stage_bytes + 31) & ~31;
+  if (rounded != e->stage_bytes) clear_graphs(e);
+  e->stage_bytes = rounded;
+  return SSE_OK;
+}
+
+int sse_get_staging(sse_engine *e, int32_t *stage_bytes) {
+  if (!e || !stage_bytes) return SSE_ERR_ARG;
+  *stage_bytes = e->stage_bytes;
+  return SSE_OK;
+}
+
 int sse_autotune(sse_engine *e, int32_t count, const int32_t *ids, int32_t nsweeps_probe, uint32_t flags,
-                 int32_t *best_warps_per_block, double *best_ms) {
+                 int32_t *best_warps_per_block, int32_t *best_stage_bytes, double *best_ms) {
   if (!e || count <= 0 || !ids || nsweeps_probe <= 0) return SSE_ERR_ARG;
-  const int candidates[3] = {1, 2, 4};
-  int best = 0;
+  for (int i = 0; i < count; i++)
+    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+  cudaSetDevice(e->device);
+  // staging budgets: off, and room for the records of the median, 90th-percentile and largest walker
+  // (25 % headroom for the operator count's fluctuations), where that fits an SM
+  std::vector<long long> n(count);
+  for (int i = 0; i < count; i++) {
+    DevWalker w;
+    int rc = read_walker(e, ids[i], w);
+    if (rc) return rc;
+    n[i] = w.n;
+  }
+  std::sort(n.begin(), n.end());
+  std::vector<int> stages{0};
+  for (double q : {0.5, 0.9, 1.0}) {
+    const long long nq = n[std::min<size_t>((size_t)count - 1, (size_t)(q * (count - 1)))];
+    const long long bytes = ((long long)(1.25 * (double)nq * sizeof(Rec)) + 1024 + 31) & ~31LL;
+    if (bytes <= SSE_MAX_STAGE_BYTES && std::find(stages.begin(), stages.end(), (int)bytes) == stages.end())
+      stages.push_back((int)bytes);
+  }
+  const int shapes[3] = {1, 2, 4};
+  int best = 0, best_stage = 0;
   double best_t = 0.0;
-  for (int c : candidates) {
-    int rc = sse_set_launch(e, c, 0);
-    if (rc) return rc;
-    rc = sse_sweep(e, count, ids, nsweeps_probe, flags & SSE_SWEEP_MEASURE);
-    if (rc) return rc;
-    if (!best || e->last_ms < best_t) {
-      best = c;
-      best_t = e->last_ms;
+  for (int st : stages) {
+    for (int c : shapes) {
+      int rc = sse_set_launch(e, c, 0);
+      if (!rc) rc = sse_set_staging(e, st);
+      if (rc) return rc;
+      int wpb, grid, spw, stage;
+      if (choose_launch(e, max_nsites_of(e, count, ids), count, wpb, grid, spw, stage, false) != SSE_OK) continue;
+      rc = sse_sweep(e, count, ids, nsweeps_probe, flags & SSE_SWEEP_MEASURE);
+      if (rc) return rc;
+      if (!best || e->last_ms < best_t) {
+        best = c;
+        best_stage = st;
+        best_t = e->last_ms;
+      }
     }
   }
+  if (!best) return fail(e, SSE_ERR_UNSUPPORTED, "no launch shape fits");
   int rc = sse_set_launch(e, best, 0);
+  if (!rc) rc = sse_set_staging(e, best_stage);
   if (rc) return rc;
   if (best_warps_per_block) *best_warps_per_block = best;
+  if (best_stage_bytes) *best_stage_bytes = best_stage;
   if (best_ms) *best_ms = best_t;
   return SSE_OK;
 }
@@ -1760,13 +1821,14 @@ extern "C" int sse_sweep_noalloc(const sse_model_desc *model, sse_noalloc_walker
   if (cudaFuncSetAttribute(k_walk<MODE_INIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
       cudaFuncSetAttribute(k_walk<MODE_SWEEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
     return SSE_ERR_CUDA;
-  k_walk<MODE_INIT><<<1, 32, spw>>>(dm, dw, nullptr, 1, 0, nullptr, flags, -1, spw, dflags);
+  k_walk<MODE_INIT><<<1, 32, spw>>>(dm, dw, nullptr, 1, 0, nullptr, flags, -1, spw, 0, dflags);
   if (cudaGetLastError() != cudaSuccess) return SSE_ERR_CUDA;
   int wst = 0;
   if (cudaMemcpyFromSymbol(&wst, g_noalloc_scratch, sizeof(int),
                            offsetof(NoAllocScratch, walker) + offsetof(DevWalker, status)) != cudaSuccess)
     return SSE_ERR_CUDA;
-  if (wst == SSE_OK) k_walk<MODE_SWEEP><<<1, 32, spw>>>(dm, dw, nullptr, 1, 0, nullptr, flags, nsweeps, spw, dflags);
+  if (wst == SSE_OK)
+    k_walk<MODE_SWEEP><<<1, 32, spw>>>(dm, dw, nullptr, 1, 0, nullptr, flags, nsweeps, spw, 0, dflags);
   k_noalloc_finish<<<1, 1>>>(X, walker);
   if (cudaGetLastError() != cudaSuccess) return SSE_ERR_CUDA;
   if (cudaMemcpyFromSymbol(&st, g_noalloc_scratch, sizeof(int), offsetof(NoAllocScratch, status)) != cudaSuccess)

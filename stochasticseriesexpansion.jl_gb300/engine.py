@@ -124,7 +124,9 @@ def lib():
             "sse_set_launch": ([eng, I32, I32], C.c_int),
             "sse_get_launch": ([eng, P(I32), P(I32)], C.c_int),
             "sse_profiler_range": ([eng, I32], C.c_int),
-            "sse_autotune": ([eng, I32, P(I32), I32, U32, P(I32), P(C.c_double)], C.c_int),
+            "sse_autotune": ([eng, I32, P(I32), I32, U32, P(I32), P(I32), P(C.c_double)], C.c_int),
+            "sse_set_staging": ([eng, I32], C.c_int),
+            "sse_get_staging": ([eng, P(I32)], C.c_int),
             "sse_walker_set_T": ([eng, I32, C.c_double], C.c_int),
             "sse_tempering_exchange": ([eng, I32, I32, P(I32), C.c_uint64, C.c_uint64, P(I32)], C.c_int),
             "sse_sweep_tempering": ([eng, I32, I32, P(I32), I32, I32, C.c_uint64, C.c_uint64, U32, P(I64), P(I64)],
@@ -148,6 +150,7 @@ def exported_symbols():
         "sse_sweep", "sse_sweep_each", "sse_observables", "sse_walker_info_get", "sse_walker_export", "sse_walker_import",
         "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range", "sse_autotune",
         "sse_sweep_noalloc", "sse_walker_set_T", "sse_tempering_exchange", "sse_sweep_tempering",
+        "sse_set_staging", "sse_get_staging",
     ]
 
 
@@ -336,13 +339,24 @@ class Engine:
         return ms.value, n.value
 
     def autotune(self, ids, nsweeps_probe: int = 5, measure: bool = False):
-        """Pick the fastest walkers-per-block for these walkers (the probe sweeps are real Carlo steps)."""
+        """Pick the fastest walkers-per-block and shared-memory staging budget for these walkers (the
+        probe sweeps are real Carlo steps); returns (walkers per block, staging bytes, probe ms)."""
         a, p = _ids(ids)
         best = C.c_int32()
+        stage = C.c_int32()
         ms = C.c_double()
         self._check(self._L.sse_autotune(self.h, len(a), p, int(nsweeps_probe), SSE_SWEEP_MEASURE if measure else 0,
-                                         C.byref(best), C.byref(ms)))
-        return best.value, ms.value
+                                         C.byref(best), C.byref(stage), C.byref(ms)))
+        return best.value, stage.value, ms.value
+
+    def set_staging(self, stage_bytes: int):
+        """Shared-memory budget per walker for staging the worm update's records (0: off)."""
+        self._check(self._L.sse_set_staging(self.h, int(stage_bytes)))
+
+    def get_staging(self) -> int:
+        v = C.c_int32()
+        self._check(self._L.sse_get_staging(self.h, C.byref(v)))
+        return v.value
 
     def profiler_range(self, start: bool):
         self._check(self._L.sse_profiler_range(self.h, int(bool(start))))

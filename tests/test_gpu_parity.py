@@ -242,13 +242,56 @@ def test_gpu_autotune_keeps_parity(S, O, eng):
     mid = eng.register_model(flat)
     ids = eng.create_walkers(mid, [dict(T=0.3, seed=8, stream=k, thermalization=50) for k in range(6)])
     eng.init(ids)
-    best, ms = eng.autotune(ids, nsweeps_probe=3)
-    assert best in (1, 2, 4) and ms > 0
+    best, stage, ms = eng.autotune(ids, nsweeps_probe=3)
+    assert best in (1, 2, 4) and stage >= 0 and ms > 0
     eng.sweep(ids, 4, measure=True)
     eng.set_launch(0, 0)
+    eng.set_staging(0)
     om = O.OracleModel(flat)
     for k, wid in enumerate(ids.tolist()):
+        done = eng.info(wid)["sweeps"]  # probe sweeps (3 per candidate) + 4
+        assert done >= 3 * 3 + 4 and (done - 4) % 3 == 0
         w = O.OracleWalker(om, T=0.3, seed=8, stream=k, thermalization=50)
         w.init()
-        w.run(3 * 3 + 4, measure=True)
+        w.run(done, measure=True)
         compare(eng, O, flat, wid, w)
+
+
+@pytest.mark.parametrize("name,T,stage", [("sq8", 0.5, 4096), ("sq8", 0.5, 192 * 1024), ("honey", 0.1, 16384),
+                                          ("bilayer", 0.25, 32768), ("cluster", 0.3, 65536), ("sq4", 4.0, 2048)])
+def test_gpu_shared_memory_staging_matches_oracle(S, O, eng, name, T, stage):
+    """Walkers whose records fit the staging budget run the worm update in shared memory; the rest
+    (and the same walker in sweeps where its operator count exceeds the budget) chase through HBM.
+    Either way the chain is the oracle's, bit for bit, including cutoff growth from a tiny start."""
+    flat = flat_of(S, name)
+    mid = eng.register_model(flat)
+    params = [dict(T=T, seed=17, stream=k, thermalization=6, init_opstring_cutoff=0 if k == 0 else -1)
+              for k in range(4)]
+    ids = eng.create_walkers(mid, params)
+    eng.init(ids)
+    eng.set_staging(stage)
+    try:
+        eng.sweep(ids, 9, measure=True)
+        eng.sweep(ids, 7, measure=True, plain=True)
+        eng.sweep(ids, 5, measure=True, graph=True)
+    finally:
+        eng.set_staging(0)
+    om = O.OracleModel(flat)
+    for p, wid in zip(params, ids.tolist()):
+        w = O.OracleWalker(om, T=T, seed=17, stream=p["stream"], thermalization=6)
+        w.init(init_cutoff=p["init_opstring_cutoff"])
+        w.run(21, measure=True)
+        compare(eng, O, flat, wid, w)
+
+
+def test_gpu_staging_argument_checks(eng):
+    from sse_gb300.engine import SSEError
+
+    with pytest.raises(SSEError):
+        eng.set_staging(-1)
+    with pytest.raises(SSEError):
+        eng.set_staging(10**7)
+    eng.set_staging(1000)
+    assert eng.get_staging() == 1024  # rounded to 32 bytes
+    eng.set_staging(0)
+    assert eng.get_staging() == 0
