@@ -340,24 +340,16 @@ def run_other_workload(args):
                     gpu_persistent_staged_sweeps_per_s=n / (ms_staged / 1e3),
                     gpu_plain_sweeps_per_s=500 / plain_s, cpu_oracle_one_core_sweeps_per_s=n / cpu_s,
                     mean_L=eng.info(int(a))["L"])
-    elif args.workload in ("uneven", "bilayer"):
-        groups = []
-        if args.workload == "uneven":
-            sides, betas = [8, 16, 24, 32, 48, 64], [0.5, 1, 2, 4, 8, 16, 32, 64]
-            nw = 8192
-            pick = [(int(rng.choice(sides)), float(rng.choice(betas))) for _ in range(nw)]
-            models = {L: eng.register_model(S.flatten_model(make_model(S, L))) for L in sides}
-            params = [(models[L], dict(T=1.0 / b, seed=args.seed, stream=k, thermalization=10**9))
-                      for k, (L, b) in enumerate(pick)]
-            desc = "8192 walkers, S=1/2 Heisenberg square L in {8..64}, beta in {0.5..64} uniform from a seed"
-        else:
-            p = {"lattice": {"unitcell": S.UnitCells.square_bilayer, "size": (48, 48)}, "S": 1.0, "J": 1.0, "Jp": 0.5,
-                 "parameter_map": {"J": ["Jp", "J", "J", "J", "J"]}, "Dz": 0.3, "hz": 0.2, "measure": ["magnetization"]}
-            mid = eng.register_model(S.flatten_model(S.MagnetModel(p)))
-            betas = [4.0, 8.0, 16.0]
-            params = [(mid, dict(T=1.0 / betas[k % 3], seed=args.seed, stream=k, thermalization=10**9))
-                      for k in range(2048)]
-            desc = "2048 walkers, S=1 square bilayer 48x48, J=1, J_perp=0.5, Dz=0.3, hz=0.2, beta in {4,8,16}"
+    elif args.workload == "uneven":
+        line.update(run_uneven_balanced(S, eng, args, rng))
+    elif args.workload == "bilayer":
+        p = {"lattice": {"unitcell": S.UnitCells.square_bilayer, "size": (48, 48)}, "S": 1.0, "J": 1.0, "Jp": 0.5,
+             "parameter_map": {"J": ["Jp", "J", "J", "J", "J"]}, "Dz": 0.3, "hz": 0.2, "measure": ["magnetization"]}
+        mid = eng.register_model(S.flatten_model(S.MagnetModel(p)))
+        betas = [4.0, 8.0, 16.0]
+        params = [(mid, dict(T=1.0 / betas[k % 3], seed=args.seed, stream=k, thermalization=10**9))
+                  for k in range(2048)]
+        desc = "2048 walkers, S=1 square bilayer 48x48, J=1, J_perp=0.5, Dz=0.3, hz=0.2, beta in {4,8,16}"
         ids = []
         for m in sorted({m for m, _ in params}):
             ids += eng.create_walkers(m, [q for mm, q in params if mm == m]).tolist()
@@ -390,6 +382,76 @@ def run_other_workload(args):
         line.update(run_reference_job(S, eng, args))
     eng.close()
     print(json.dumps(line), flush=True)
+
+
+def run_uneven_balanced(S, eng, args, rng):
+    """8192 walkers of S=1/2 Heisenberg square lattices, side L in {8,...,64} and beta in {0.5,...,64}
+    drawn uniformly from a seed.  A step is one cost-balanced block (sse_sweep_each): walker i runs
+    k_i = round(c_max / c_i) sweeps (1 <= k_i <= 4096), c_i its device clock cycles per sweep measured in
+    the previous block, so that every walker works for about as long as one sweep of the slowest; the
+    launch shape and shared-memory staging budget come from sse_autotune_each on such a block."""
+    from sse_gb300.engine import SSEError
+
+    sides, betas = [8, 16, 24, 32, 48, 64], [0.5, 1, 2, 4, 8, 16, 32, 64]
+    nw = 8192
+    pick = [(int(rng.choice(sides)), float(rng.choice(betas))) for _ in range(nw)]
+    models = {L: eng.register_model(S.flatten_model(make_model(S, L))) for L in sides}
+    ids = np.zeros(nw, dtype=np.int32)
+    for L in sides:
+        sel = [k for k, (l, _) in enumerate(pick) if l == L]
+        got = eng.create_walkers(models[L], [dict(T=1.0 / pick[k][1], seed=args.seed, stream=k, thermalization=0)
+                                             for k in sel])
+        ids[sel] = got
+    eng.init(ids)
+
+    def counters():
+        inf = [eng.info(int(i)) for i in ids]
+        return (np.array([x["slot_visits"] + x["worm_steps"] for x in inf], dtype=np.float64),
+                np.array([x["sweeps"] for x in inf], dtype=np.int64), np.array([x["L"] for x in inf]),
+                np.array([sum(x["phase_cycles"]) for x in inf], dtype=np.float64))
+
+    def block(k, measure):
+        try:
+            eng.sweep_each(ids, k, measure=measure)
+        except SSEError as err:
+            raise RuntimeError(f"uneven batch: {err}")
+        return eng.last_timing()[0] / 1e3
+
+    t0 = time.perf_counter()
+    _, sw0, _, cy0 = counters()
+    block(np.ones(nw, dtype=np.int32), False)
+    _, sw1, _, cy1 = counters()
+
+    def balanced(sw_a, cy_a, sw_b, cy_b):
+        # device clock cycles per sweep of every walker in the last block (its latency under load)
+        cost = (cy_b - cy_a) / np.maximum(sw_b - sw_a, 1)
+        return np.clip(np.rint(cost.max() / np.maximum(cost, 1.0)), 1, 4096).astype(np.int32)
+
+    k = balanced(sw0, cy0, sw1, cy1)
+    for _ in range(max(args.warmup, 3)):
+        sw0, cy0 = sw1, cy1
+        block(k, False)
+        _, sw1, _, cy1 = counters()
+        k = balanced(sw0, cy0, sw1, cy1)
+    warm_s = time.perf_counter() - t0
+    best_wpb, best_stage, probe_ms = eng.autotune_each(ids, k, measure=False)
+    ou0, sw0, _, cy0 = counters()
+    dev = 0.0
+    ou_start, sw_start = ou0, sw0
+    for _ in range(args.steps):
+        dev += block(k, True)
+        ou1, sw1, Ls, cy1 = counters()
+        k = balanced(sw0, cy0, sw1, cy1)
+        sw0, cy0 = sw1, cy1
+    ws = float((sw1 - sw_start).sum())
+    ou = float((ou1 - ou_start).sum())
+    return dict(config="8192 walkers, S=1/2 Heisenberg square L in {8..64}, beta in {0.5..64} uniform from a seed; "
+                       "cost-balanced blocks (sse_sweep_each)",
+                steps=args.steps, warmup_blocks=max(args.warmup, 3), warmup_seconds=warm_s,
+                walker_sweeps_per_s=ws / dev, operator_updates_per_s=ou / dev,
+                sweeps_per_block_min_median_max=[int(k.min()), int(np.median(k)), int(k.max())],
+                autotuned_warps_per_block=best_wpb, autotuned_stage_bytes=best_stage,
+                cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
 
 
 def reference_job_model(S, name):

@@ -186,11 +186,16 @@ int sse_get_launch(sse_engine *eng, int32_t *warps_per_block, int32_t *blocks_pe
 int sse_set_staging(sse_engine *eng, int32_t stage_bytes);
 int sse_get_staging(sse_engine *eng, int32_t *stage_bytes);
 /* times nsweeps_probe sweeps of the given walkers for each launch shape (1, 2, 4 walkers per block)
- * and staging budget (off, and room for the median, 90th-percentile and largest walker's records)
+ * and staging budget (off, 8 KB, 32 KB, and room for the 25th-percentile, median and largest walker's
+ * records)
  * and keeps the fastest; the probe sweeps are ordinary Carlo steps of those walkers (run it during
  * thermalisation) */
 int sse_autotune(sse_engine *eng, int32_t count, const int32_t *ids, int32_t nsweeps_probe, uint32_t flags,
                  int32_t *best_warps_per_block, int32_t *best_stage_bytes, double *best_ms);
+/* as sse_autotune, each probe an sse_sweep_each with nsweeps[i] Carlo steps for walker i (the
+ * cost-balanced blocks of an uneven batch) */
+int sse_autotune_each(sse_engine *eng, int32_t count, const int32_t *ids, const int32_t *nsweeps, uint32_t flags,
+                      int32_t *best_warps_per_block, int32_t *best_stage_bytes, double *best_ms);
 /* brackets a profiled region (cudaProfilerStart / cudaProfilerStop) for profilers started with
  * collection off; start != 0 opens the region, 0 closes it */
 int sse_profiler_range(sse_engine *eng, int32_t start);

@@ -1319,14 +1319,21 @@ int sse_get_staging(sse_engine *e, int32_t *stage_bytes) {
   return SSE_OK;
 }
 
-int sse_autotune(sse_engine *e, int32_t count, const int32_t *ids, int32_t nsweeps_probe, uint32_t flags,
-                 int32_t *best_warps_per_block, int32_t *best_stage_bytes, double *best_ms) {
-  if (!e || count <= 0 || !ids || nsweeps_probe <= 0) return SSE_ERR_ARG;
+}  // extern "C"
+
+namespace {
+
+// Probes every launch shape and staging budget with real sweeps of the given walkers: nsweeps_probe
+// each (sse_sweep), or nsweeps_each[i] for walker i (sse_sweep_each) when that array is given.
+int autotune_impl(sse_engine *e, int32_t count, const int32_t *ids, int32_t nsweeps_probe,
+                  const int32_t *nsweeps_each, uint32_t flags, int32_t *best_warps_per_block,
+                  int32_t *best_stage_bytes, double *best_ms) {
+  if (!e || count <= 0 || !ids || (!nsweeps_each && nsweeps_probe <= 0)) return SSE_ERR_ARG;
   for (int i = 0; i < count; i++)
     if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
   cudaSetDevice(e->device);
-  // staging budgets: off, and room for the records of the median, 90th-percentile and largest walker
-  // (25 % headroom for the operator count's fluctuations), where that fits an SM
+  // staging budgets: off, 8 and 32 KB, and room for the records of the 25th-percentile, median and
+  // largest walker (25 % headroom for the operator count's fluctuations), where that fits an SM
   std::vector<long long> n(count);
   for (int i = 0; i < count; i++) {
     DevWalker w;
@@ -1335,8 +1342,8 @@ int sse_autotune(sse_engine *e, int32_t count, const int32_t *ids, int32_t nswee
     n[i] = w.n;
   }
   std::sort(n.begin(), n.end());
-  std::vector<int> stages{0};
-  for (double q : {0.5, 0.9, 1.0}) {
+  std::vector<int> stages{0, 8192, 32768};
+  for (double q : {0.25, 0.5, 1.0}) {
     const long long nq = n[std::min<size_t>((size_t)count - 1, (size_t)(q * (count - 1)))];
     const long long bytes = ((long long)(1.25 * (double)nq * sizeof(Rec)) + 1024 + 31) & ~31LL;
     if (bytes <= SSE_MAX_STAGE_BYTES && std::find(stages.begin(), stages.end(), (int)bytes) == stages.end())
@@ -1352,7 +1359,8 @@ int sse_autotune(sse_engine *e, int32_t count, const int32_t *ids, int32_t nswee
       if (rc) return rc;
       int wpb, grid, spw, stage;
       if (choose_launch(e, max_nsites_of(e, count, ids), count, wpb, grid, spw, stage, false) != SSE_OK) continue;
-      rc = sse_sweep(e, count, ids, nsweeps_probe, flags & SSE_SWEEP_MEASURE);
+      rc = nsweeps_each ? sse_sweep_each(e, count, ids, nsweeps_each, flags & SSE_SWEEP_MEASURE)
+                        : sse_sweep(e, count, ids, nsweeps_probe, flags & SSE_SWEEP_MEASURE);
       if (rc) return rc;
       if (!best || e->last_ms < best_t) {
         best = c;
@@ -1369,6 +1377,22 @@ int sse_autotune(sse_engine *e, int32_t count, const int32_t *ids, int32_t nswee
   if (best_stage_bytes) *best_stage_bytes = best_stage;
   if (best_ms) *best_ms = best_t;
   return SSE_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sse_autotune(sse_engine *e, int32_t count, const int32_t *ids, int32_t nsweeps_probe, uint32_t flags,
+                 int32_t *best_warps_per_block, int32_t *best_stage_bytes, double *best_ms) {
+  return autotune_impl(e, count, ids, nsweeps_probe, nullptr, flags, best_warps_per_block, best_stage_bytes,
+                       best_ms);
+}
+
+int sse_autotune_each(sse_engine *e, int32_t count, const int32_t *ids, const int32_t *nsweeps, uint32_t flags,
+                      int32_t *best_warps_per_block, int32_t *best_stage_bytes, double *best_ms) {
+  if (!nsweeps) return SSE_ERR_ARG;
+  return autotune_impl(e, count, ids, 0, nsweeps, flags, best_warps_per_block, best_stage_bytes, best_ms);
 }
 
 int sse_get_launch(sse_engine *e, int32_t *warps_per_block, int32_t *blocks_per_sm) {

@@ -125,6 +125,7 @@ def lib():
             "sse_get_launch": ([eng, P(I32), P(I32)], C.c_int),
             "sse_profiler_range": ([eng, I32], C.c_int),
             "sse_autotune": ([eng, I32, P(I32), I32, U32, P(I32), P(I32), P(C.c_double)], C.c_int),
+            "sse_autotune_each": ([eng, I32, P(I32), P(I32), U32, P(I32), P(I32), P(C.c_double)], C.c_int),
             "sse_set_staging": ([eng, I32], C.c_int),
             "sse_get_staging": ([eng, P(I32)], C.c_int),
             "sse_walker_set_T": ([eng, I32, C.c_double], C.c_int),
@@ -150,7 +151,7 @@ def exported_symbols():
         "sse_sweep", "sse_sweep_each", "sse_observables", "sse_walker_info_get", "sse_walker_export", "sse_walker_import",
         "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range", "sse_autotune",
         "sse_sweep_noalloc", "sse_walker_set_T", "sse_tempering_exchange", "sse_sweep_tempering",
-        "sse_set_staging", "sse_get_staging",
+        "sse_set_staging", "sse_get_staging", "sse_autotune_each",
     ]
 
 
@@ -347,6 +348,20 @@ class Engine:
         ms = C.c_double()
         self._check(self._L.sse_autotune(self.h, len(a), p, int(nsweeps_probe), SSE_SWEEP_MEASURE if measure else 0,
                                          C.byref(best), C.byref(stage), C.byref(ms)))
+        return best.value, stage.value, ms.value
+
+    def autotune_each(self, ids, nsweeps, measure: bool = False):
+        """As autotune, each probe giving walker i nsweeps[i] Carlo steps (cost-balanced blocks)."""
+        a, p = _ids(ids)
+        ns = np.ascontiguousarray(nsweeps, dtype=np.int32)
+        if len(ns) != len(a):
+            raise ValueError("one sweep count per walker")
+        best = C.c_int32()
+        stage = C.c_int32()
+        ms = C.c_double()
+        self._check(self._L.sse_autotune_each(self.h, len(a), p, _p(ns, C.c_int32),
+                                              SSE_SWEEP_MEASURE if measure else 0, C.byref(best), C.byref(stage),
+                                              C.byref(ms)))
         return best.value, stage.value, ms.value
 
     def set_staging(self, stage_bytes: int):

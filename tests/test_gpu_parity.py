@@ -242,7 +242,7 @@ def test_gpu_autotune_keeps_parity(S, O, eng):
     mid = eng.register_model(flat)
     ids = eng.create_walkers(mid, [dict(T=0.3, seed=8, stream=k, thermalization=50) for k in range(6)])
     eng.init(ids)
-    best, stage, ms = eng.autotune(ids, nsweeps_probe=3)
+    best, stage, ms = eng.autotune(ids, nsweeps_probe=3, measure=True)
     assert best in (1, 2, 4) and stage >= 0 and ms > 0
     eng.sweep(ids, 4, measure=True)
     eng.set_launch(0, 0)
@@ -295,3 +295,25 @@ def test_gpu_staging_argument_checks(eng):
     assert eng.get_staging() == 1024  # rounded to 32 bytes
     eng.set_staging(0)
     assert eng.get_staging() == 0
+
+
+def test_gpu_autotune_each_keeps_parity(S, O, eng):
+    """Probing launch shapes and staging budgets with per-walker sweep counts runs real Carlo steps:
+    every walker ends exactly where the oracle does after the same number of steps."""
+    flat = flat_of(S, "sq4")
+    mid = eng.register_model(flat)
+    ids = eng.create_walkers(mid, [dict(T=0.4, seed=31, stream=k, thermalization=5) for k in range(5)])
+    eng.init(ids)
+    ns = np.array([1, 3, 2, 1, 4], dtype=np.int32)
+    best, stage, ms = eng.autotune_each(ids, ns, measure=True)
+    assert best in (1, 2, 4) and stage >= 0 and ms > 0
+    eng.set_launch(0, 0)
+    eng.set_staging(0)
+    om = O.OracleModel(flat)
+    nprobe = eng.info(int(ids[0]))["sweeps"] // int(ns[0])
+    for k, wid in enumerate(ids.tolist()):
+        assert eng.info(wid)["sweeps"] == nprobe * int(ns[k])
+        w = O.OracleWalker(om, T=0.4, seed=31, stream=k, thermalization=5)
+        w.init()
+        w.run(nprobe * int(ns[k]), measure=True)
+        compare(eng, O, flat, wid, w)
