@@ -12,7 +12,12 @@ unmeasured).  The loop
   in one persistent launch per tick (`sse_sweep_each`), so requests that
   arrive while others run join the next launch,
 * retires a request as soon as its walkers are done, reporting its
-  observables and its time-to-result (completion - arrival).
+  observables and its time-to-result (completion - arrival),
+* replaces a walker that the engine stopped (a worm that never closed,
+  SSE_ERR_WORM_CAP) with a fresh chain, up to `retries` times per walker:
+  slot k of a request runs stream k, its a-th replacement stream
+  k + a * nwalkers, each replacement all of the request's sweeps from
+  init!; with retries exhausted the request is reported as failed.
 
 A walker's trajectory depends only on its own (seed, stream), so a request's
 result is the same whether it runs alone or mixed with others.
@@ -61,6 +66,7 @@ class Result:
     operator_updates: int = 0
     energy: float = float("nan")
     status: str = "ok"  # or the sse_status name that stopped one of its walkers
+    replaced: int = 0  # walkers replaced by a fresh chain after the engine stopped them
 
     @property
     def latency(self) -> float:
@@ -126,9 +132,12 @@ def draw_requests(seed: int, count: int, rate: float = 200.0, side=(8, 64), beta
 class _Active:
     req: Request
     ids: np.ndarray
-    done: int = 0
+    done: np.ndarray  # sweeps done, per walker
     nbytes: int = 0
     cost: float = 1.0  # projected operator-updates per sweep of one walker
+    attempts: np.ndarray = None  # replacements so far, per walker slot
+    replaced: int = 0
+    spent_updates: int = 0  # operator-updates of walkers that were replaced
 
 
 class ServingLoop:
@@ -138,8 +147,9 @@ class ServingLoop:
     it every walker gets `tick_sweeps` sweeps per tick."""
 
     def __init__(self, engine, memory_budget: int, tick_sweeps: int = 10, clock=time.perf_counter,
-                 tick_seconds: float | None = None, walker_rate: float = 1.5e6):
+                 tick_seconds: float | None = None, walker_rate: float = 1.5e6, retries: int = 2):
         self.eng = engine
+        self.retries = int(retries)
         self.budget = int(memory_budget)
         self.tick = int(tick_sweeps)
         self.tick_seconds = tick_seconds
@@ -175,18 +185,23 @@ class ServingLoop:
             if self.active and self.used + need > self.budget:
                 break
             self.pending.pop(0)
-            mid, flat = self._model(req.model_key)
-            params = [dict(T=1.0 / req.beta, seed=req.seed, stream=k, thermalization=req.thermalization)
-                      for k in range(req.nwalkers)]
-            ids = self.eng.create_walkers(mid, params)
-            if hasattr(self.eng, "reserve"):
-                self.eng.reserve(ids, projected_slots(req.S, req.lattice, req.side, req.beta))
-            self.eng.init(ids)
+            ids = self._new_walkers(req, list(range(req.nwalkers)))
             cost = projected_sweep_cost(req.S, req.lattice, req.side, req.beta)
-            self.active.append(_Active(req, ids, 0, need, cost))
+            self.active.append(_Active(req, ids, np.zeros(req.nwalkers, dtype=np.int64), need, cost,
+                                       np.zeros(req.nwalkers, dtype=np.int64)))
             self.used += need
             admitted.append(req.rid)
         return admitted
+
+    def _new_walkers(self, req: Request, streams):
+        mid, flat = self._model(req.model_key)
+        params = [dict(T=1.0 / req.beta, seed=req.seed, stream=int(k), thermalization=req.thermalization)
+                  for k in streams]
+        ids = self.eng.create_walkers(mid, params)
+        if hasattr(self.eng, "reserve"):
+            self.eng.reserve(ids, projected_slots(req.S, req.lattice, req.side, req.beta))
+        self.eng.init(ids)
+        return np.asarray(ids, dtype=np.int32)
 
     def step(self):
         """One tick: every active walker advances min(tick, remaining) sweeps in one launch."""
@@ -195,26 +210,42 @@ class ServingLoop:
         ids, ns = [], []
         planned = 0.0
         for a in self.active:
+            left = a.req.nsweeps - a.done
             if self.tick_seconds:
-                k = int(max(1, min(a.req.nsweeps - a.done, self.tick_seconds * self.rate / a.cost)))
+                k = np.maximum(1, np.minimum(left, int(max(1, self.tick_seconds * self.rate / a.cost))))
             else:
-                k = min(self.tick, a.req.nsweeps - a.done)
-            planned = max(planned, k * a.cost)
+                k = np.minimum(self.tick, left)
+            k = np.where(left > 0, k, 0)
+            planned = max(planned, float(k.max()) * a.cost)
             ids.append(a.ids)
-            ns.append(np.full(len(a.ids), k, dtype=np.int32))
+            ns.append(k.astype(np.int32))
             a.done += k
         failed = {}
         t_start = self.clock()
         try:
             self.eng.sweep_each(np.concatenate(ids), np.concatenate(ns), measure=True)
         except SSEError as err:
-            # every other walker finished its sweeps; find the requests whose walkers stopped
+            # every other walker finished its sweeps; replace the walkers that stopped, or fail
+            # their request when its replacements are used up
+            stopped = 0
             for a in self.active:
-                for i in a.ids.tolist():
+                for slot, i in enumerate(a.ids.tolist()):
                     st = self.eng.info(i)["status"]
-                    if st != 0:
+                    if st == 0:
+                        continue
+                    stopped += 1
+                    if a.attempts[slot] < self.retries:
+                        a.attempts[slot] += 1
+                        inf = self.eng.info(i)
+                        a.spent_updates += inf["slot_visits"] + inf["worm_steps"]
+                        self.eng.destroy_walkers(np.array([i], dtype=np.int32))
+                        stream = slot + int(a.attempts[slot]) * a.req.nwalkers
+                        a.ids[slot] = self._new_walkers(a.req, [stream])[0]
+                        a.done[slot] = 0
+                        a.replaced += 1
+                    else:
                         failed[a.req.rid] = STATUS_NAMES.get(st, str(st))
-            if not failed:
+            if not stopped:
                 raise err
         self.launches += 1
         took = self.clock() - t_start
@@ -223,7 +254,7 @@ class ServingLoop:
         finished = []
         still = []
         for a in self.active:
-            if a.done >= a.req.nsweeps or a.req.rid in failed:
+            if (a.done >= a.req.nsweeps).all() or a.req.rid in failed:
                 finished.append(a)
             else:
                 still.append(a)
@@ -234,7 +265,7 @@ class ServingLoop:
             obs = self.eng.observables(a.ids)
             sums = np.array([o[0] for o in obs])
             counts = np.array([o[1] for o in obs])
-            ou = 0
+            ou = a.spent_updates
             for i in a.ids.tolist():
                 inf = self.eng.info(i)
                 ou += inf["slot_visits"] + inf["worm_steps"]
@@ -248,7 +279,7 @@ class ServingLoop:
             c = counts.sum(0)
             energy = (s[4] / c[4]) / (s[0] / c[0]) if (c[0] and c[4] and s[0]) else float("nan")
             res = Result(a.req.rid, a.req.arrival, t, names, sums, counts, ou, energy,
-                         status=failed.get(a.req.rid, "ok"))
+                         status=failed.get(a.req.rid, "ok"), replaced=a.replaced)
             self.results.append(res)
             out.append(res)
         return out
@@ -279,6 +310,7 @@ class ServingLoop:
         return {
             "requests": len(self.results),
             "failed": sum(r.status != "ok" for r in self.results),
+            "walkers_replaced": sum(r.replaced for r in self.results),
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "mean_s": float(lat.mean()) if len(lat) else None,

@@ -76,3 +76,68 @@ def test_request_draw_distribution(S):
     assert all(8 <= r.side <= 64 and 0.5 <= r.beta <= 64 and 1 <= r.nwalkers <= 64 for r in reqs)
     assert all(1000 <= r.nsweeps <= 10000 for r in reqs)
     assert draw_requests(7, 5)[3] == draw_requests(7, 5)[3]
+
+
+class TrapEngine(FakeEngine):
+    """Stops the walker of stream `trap_stream` once, at its `trap_at`-th sweep, like a worm that never
+    closed (SSE_ERR_WORM_CAP)."""
+
+    def __init__(self, trap_stream, trap_at):
+        super().__init__()
+        self.trap_stream, self.trap_at = trap_stream, trap_at
+        self.status = {}
+
+    def sweep_each(self, ids, ns, measure=True):
+        from sse_gb300.engine import SSEError
+
+        self.calls.append((list(ids), list(ns)))
+        hit = False
+        for i, n in zip(ids.tolist(), ns.tolist()):
+            w = self.walkers[i]
+            if self.status.get(i, 0):
+                continue
+            if w["p"]["stream"] == self.trap_stream and w["sweeps"] < self.trap_at <= w["sweeps"] + n:
+                w["sweeps"] = self.trap_at
+                self.status[i] = 8
+                hit = True
+            else:
+                w["sweeps"] += n
+        if hit:
+            raise SSEError(8, "walker stopped with status 8")
+
+    def info(self, i):
+        d = super().info(i)
+        d["status"] = self.status.get(i, 0)
+        return d
+
+    def create_walkers(self, mid, params):
+        self.created = getattr(self, "created", []) + [p["stream"] for p in params]
+        return super().create_walkers(mid, params)
+
+
+def test_stopped_walker_is_replaced_by_a_fresh_chain(S):
+    from sse_gb300.serving import Request, ServingLoop
+
+    eng = TrapEngine(trap_stream=1, trap_at=17)
+    req = Request(0, 0.0, 1.0, "square", 4, 1.0, nwalkers=3, nsweeps=40, seed=5)
+    loop = ServingLoop(eng, memory_budget=10**12, tick_sweeps=10, clock=iter(np.arange(0, 1e6, 0.5)).__next__)
+    (res,) = loop.run([req], realtime=False)
+    assert res.status == "ok" and res.replaced == 1
+    # slot 1's replacement ran stream 1 + 1*3 = 4 for all 40 sweeps, from init!
+    assert eng.created == [0, 1, 2, 4]
+    assert not eng.walkers  # all retired
+    assert np.all(res.sums[:, 0] == 40)
+    assert res.operator_updates == 3 * 40 * 15 + 17 * 15  # the stopped walker's work is counted too
+    assert loop.summary()["walkers_replaced"] == 1
+
+
+def test_request_fails_when_replacements_are_used_up(S):
+    from sse_gb300.serving import Request, ServingLoop
+
+    eng = TrapEngine(trap_stream=0, trap_at=3)
+    req = Request(0, 0.0, 1.0, "square", 4, 1.0, nwalkers=2, nsweeps=20, seed=5)
+    loop = ServingLoop(eng, memory_budget=10**12, tick_sweeps=10, retries=0,
+                       clock=iter(np.arange(0, 1e6, 0.5)).__next__)
+    (res,) = loop.run([req], realtime=False)
+    assert res.status == "SSE_ERR_WORM_CAP" and res.replaced == 0
+    assert loop.summary()["failed"] == 1
