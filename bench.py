@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--therm", type=int, default=2000, help="thermalisation sweeps before the warm-up steps")
     ap.add_argument("--sweeps-per-step", type=int, default=50)
     ap.add_argument("--plain-walkers", type=int, default=8)
-    ap.add_argument("--cpu-sweeps", type=int, default=20, help="sweeps per chain in the CPU baseline sample")
+    ap.add_argument("--cpu-sweeps", type=int, default=2000,
+                    help="sweeps per chain in the CPU baseline sample (about 10 s on 16 cores for the default workload)")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--seed", type=int, default=20261203)
     ap.add_argument("--profile", action="store_true", help="open a profiler range around the timed steps only")
