@@ -113,7 +113,7 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
         const long long nrec = build_links(M, c.L, ops, W->rec, W->cidx, W->vfirst, vlast, lane);
         // records that fit the staging budget move to shared memory for the pointer chase
         Rec *wrec = W->rec;
-        const bool staged = nrec * (long long)sizeof(Rec) <= (long long)stage_bytes;
+        const bool staged = stage_bytes > 0 && nrec * (long long)sizeof(Rec) <= (long long)stage_bytes;
         if (staged) {
           int4 *dst = reinterpret_cast<int4 *>(smem + (smem_per_warp - stage_bytes));
           const int4 *src = reinterpret_cast<const int4 *>(W->rec);
