@@ -66,19 +66,24 @@ struct DevModel {
 // Scatter tables (src/vertex_data.jl:106-125) with integer thresholds: for
 // r = u53 * 2^-53 (u53 = u >> 11) the reference's test `r < cum` holds
 // exactly when u53 < ceil(cum * 2^53), so the worm compares integers.
-// packed = leg_out | worm_out << 2 | target vertex code << 10.
+// packed = leg_out | worm_out << 2 | target vertex code << 10 | dim_out << 20,
+// dim_out the dimension of the site of leg_out (the worm's closing test).
 struct __align__(16) Outcome {
   unsigned long long thr;
   int32_t packed;
   int32_t pad;
 };
 
-// A transition row with its first outcome inline; `rest` = index of the
-// second outcome << 8 | number of further outcomes.  packed0 < 0: invalid.
-struct __align__(16) Trans {
+// A transition row with its first two outcomes inline (packed1 < 0: the row has
+// one); `rest` = index of the third outcome << 8 | number of further outcomes.
+// packed0 < 0: invalid row.
+struct __align__(32) Trans {
   unsigned long long thr0;
   int32_t packed0;
   int32_t rest;
+  unsigned long long thr1;
+  int32_t packed1;
+  int32_t pad;
 };
 
 // One non-identity operator of the compacted opstring, 32 bytes = one DRAM
@@ -678,6 +683,8 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
     const Trans tr = trans[ti];
     int packed = tr.packed0;
     if (packed >= 0 && !(u53 < tr.thr0)) {
+      packed = tr.packed1;
+      if (packed >= 0 && !(u53 < tr.thr1)) {
       packed = -1;
       const int o0 = tr.rest >> 8, on = tr.rest & 0xFF;
       for (int o = o0; o < o0 + on; o++) {
@@ -687,6 +694,7 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
           break;
         }
       }
+      }
     }
     if (packed < 0) {
       status = ST_INVALID_VERTEX;
@@ -694,10 +702,10 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
     }
     const int leg_out = packed & 3;
     const int wf_out = (packed >> 2) & 0xFF;
-    const uint32_t nop = 1u | ((uint32_t)(packed >> 10) << 1) | (op & 0xFFFFF800u);
+    const uint32_t nop = 1u | ((uint32_t)((packed >> 10) & 0x3FF) << 1) | (op & 0xFFFFF800u);
     const int slot = rb.y;
     const int kcur = k;
-    const int dim_out = (leg_out & 1) ? ((rb.w >> 16) & 0xFF) : ((rb.w >> 8) & 0xFF);
+    const int dim_out = (packed >> 20) & 0xFF;
     bool fin = (k == k0 && leg_out == l0 && wf_out == dim_out - wf0);
     if (!fin) {
       len += 1;

@@ -936,19 +936,38 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
     outc[o].packed = leg | (worm << 2) | (tgt << 10);
     outc[o].pad = 0;
   }
+  // the bond type of every transition row, for the dimension of each outcome's site
+  std::vector<int32_t> row_type(ntrans, -1);
+  for (int t = 0; t < d->ntypes; t++) {
+    const size_t r0 = (size_t)d->type_trans_off[t];
+    const size_t r1 = r0 + (size_t)types[t].nverts * 4 * types[t].maxworm;
+    for (size_t r = r0; r < r1 && r < ntrans; r++) row_type[r] = t;
+  }
   std::vector<Trans> trans(ntrans);
   for (size_t i = 0; i < ntrans; i++) {
     const int start = d->trans_start[i], cnt = d->trans_count[i];
-    if (start < 0 || cnt <= 0) {
-      trans[i].thr0 = 0;
-      trans[i].packed0 = -1;
-      trans[i].rest = 0;
-      continue;
+    trans[i].thr0 = 0;
+    trans[i].packed0 = -1;
+    trans[i].rest = 0;
+    trans[i].thr1 = 0;
+    trans[i].packed1 = -1;
+    trans[i].pad = 0;
+    if (start < 0 || cnt <= 0) continue;
+    if (cnt > 256 || start + 2 >= (1 << 23)) return fail(e, SSE_ERR_UNSUPPORTED, "transition row too long");
+    if ((size_t)start + (size_t)cnt > nout || row_type[i] < 0)
+      return fail(e, SSE_ERR_ARG, "transition row outside the outcome table");
+    const DevType &ty = types[row_type[i]];
+    for (int o = start; o < start + cnt; o++) {
+      const int dim_out = (outc[o].packed & 1) ? ty.d1 : ty.d0;  // leg_out & 1: the bond's second site
+      outc[o].packed = (outc[o].packed & 0xFFFFF) | (dim_out << 20);
     }
-    if (cnt > 256 || start + 1 >= (1 << 23)) return fail(e, SSE_ERR_UNSUPPORTED, "transition row too long");
     trans[i].thr0 = outc[start].thr;
     trans[i].packed0 = outc[start].packed;
-    trans[i].rest = ((start + 1) << 8) | (cnt - 1);
+    if (cnt > 1) {
+      trans[i].thr1 = outc[start + 1].thr;
+      trans[i].packed1 = outc[start + 1].packed;
+    }
+    if (cnt > 2) trans[i].rest = ((start + 2) << 8) | (cnt - 2);
   }
   if (!rc) rc = upload(e, hm, trans.data(), ntrans, &m.trans);
   if (!rc) rc = upload(e, hm, outc.data(), nout, &m.outc);
@@ -1711,10 +1730,22 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
       tr.thr0 = 0;
       tr.packed0 = -1;
       tr.rest = 0;
+      tr.thr1 = 0;
+      tr.packed1 = -1;
+      tr.pad = 0;
     } else {
+      int t = 0;
+      while (t + 1 < d.ntypes && d.type_trans_off[t + 1] <= i) t++;
+      for (int o = st; o < st + cnt; o++) {
+        const int leg = X->outc[o].packed & 3;
+        X->outc[o].packed = (X->outc[o].packed & 0xFFFFF) | (((leg & 1) ? d.type_dims[2 * t + 1] : d.type_dims[2 * t]) << 20);
+      }
       tr.thr0 = X->outc[st].thr;
       tr.packed0 = X->outc[st].packed;
-      tr.rest = ((st + 1) << 8) | (cnt - 1);
+      tr.thr1 = cnt > 1 ? X->outc[st + 1].thr : 0;
+      tr.packed1 = cnt > 1 ? X->outc[st + 1].packed : -1;
+      tr.pad = 0;
+      tr.rest = cnt > 2 ? (((st + 2) << 8) | (cnt - 2)) : 0;
     }
   }
   if (tid == 0) {
