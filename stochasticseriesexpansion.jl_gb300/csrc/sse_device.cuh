@@ -665,7 +665,10 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
   const Outcome *__restrict__ outc = M.outc;
   const int4 *rq = reinterpret_cast<const int4 *>(rec);
   int k = cs.k, leg_in = cs.leg_in, wf = cs.wf;
-  long long len = cs.len;
+  const long long len0 = cs.len;
+  // steps left before the worm exceeds the cap (a draw window has at most 64 steps)
+  const int room = (cap - len0) > 0x3FFFFFFFLL ? 0x3FFFFFFF : (int)(cap - len0);
+  int used = 0;
   int4 ra = cs.ra, rb = cs.rb;
   int status = ST_OK;
   while (pos < 64) {
@@ -708,7 +711,7 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
     const int dim_out = (packed >> 20) & 0xFF;
     bool fin = (k == k0 && leg_out == l0 && wf_out == dim_out - wf0);
     if (!fin) {
-      len += 1;
+      used += 1;
       wf = wf_out;
       const int link = leg_out == 0 ? ra.x : leg_out == 1 ? ra.y : leg_out == 2 ? ra.z : ra.w;
       leg_in = link & 3;
@@ -722,7 +725,7 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
       done = true;
       break;
     }
-    if (len > cap) {
+    if (used > room) {  // len0 + used > cap
       status = ST_WORM_CAP;
       break;
     }
@@ -732,7 +735,7 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
   cs.k = k;
   cs.leg_in = leg_in;
   cs.wf = wf;
-  cs.len = len;
+  cs.len = len0 + used;
   cs.ra = ra;
   cs.rb = rb;
   return status;
