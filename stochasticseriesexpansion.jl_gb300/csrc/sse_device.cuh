@@ -718,9 +718,10 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
       k = link >> 2;
       fin = (k == k0 && leg_in == l0 && wf == wf0);
     }
-    // the store precedes the next load of the same record, so a revisit sees the new code
+    // the store precedes the next load of the same record, so a revisit sees the new code; the
+    // opstring itself is written once after the worms (slot order, coalesced)
     rec[kcur].op = nop;
-    ops[slot] = nop;
+    (void)slot;
     if (fin) {
       done = true;
       break;
@@ -813,10 +814,23 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
     steps += (long long)(ctr - c.ctr);  // one draw per scatter
     c.ctr = ctr;
     const long long len = shfl_ll(cs.len, 0);
-    if (status != ST_OK) return status;
+    if (status != ST_OK) {
+      for (long long k = lane; k < c.n; k += 32) {
+        const int2 os = reinterpret_cast<const int2 *>(rec + k)[2];
+        ops[os.y] = (uint32_t)os.x;
+      }
+      __syncwarp();
+      return status;
+    }
     total = __dadd_rn(total, (double)len);
   }
 
+  // the operators' final codes back into the opstring (slot order, coalesced)
+  for (long long k = lane; k < c.n; k += 32) {
+    const int2 os = reinterpret_cast<const int2 *>(rec + k)[2];
+    ops[os.y] = (uint32_t)os.x;
+  }
+  __syncwarp();
   have_wlf = thermalized && c.n != 0;
   if (have_wlf) wlf = __ddiv_rn(total, (double)c.n);
 
