@@ -617,15 +617,23 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
         int wpb, grid, spw, stage;
         rc = choose_launch(e, max_ns, n, wpb, grid, spw, stage, false);
         if (rc) return rc;
-        cudaGraph_t graph;
+        cudaGraph_t graph = nullptr;
         CUDA_TRY(e, cudaStreamBeginCapture(e->stream, cudaStreamCaptureModeThreadLocal));
-        cudaMemsetAsync(e->d_flags, 0, 2 * sizeof(int), e->stream);
-        cudaMemsetAsync(e->d_queue, 0, sizeof(int), e->stream);
-        k_walk<MODE_SWEEP><<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(
-            e->d_models, e->d_walkers, g.d_work, n, -1, e->d_queue, flags, add, spw, stage, e->d_flags);
-        CUDA_TRY(e, cudaStreamEndCapture(e->stream, &graph));
-        CUDA_TRY(e, cudaGraphInstantiate(&g.exec, graph, 0));
-        cudaGraphDestroy(graph);
+        cudaError_t cst = cudaMemsetAsync(e->d_flags, 0, 2 * sizeof(int), e->stream);
+        if (cst == cudaSuccess) cst = cudaMemsetAsync(e->d_queue, 0, sizeof(int), e->stream);
+        if (cst == cudaSuccess) {
+          k_walk<MODE_SWEEP><<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(
+              e->d_models, e->d_walkers, g.d_work, n, -1, e->d_queue, flags, add, spw, stage, e->d_flags);
+          cst = cudaGetLastError();
+        }
+        const cudaError_t est = cudaStreamEndCapture(e->stream, &graph);  // always leave capture mode
+        if (cst == cudaSuccess) cst = est;
+        if (cst == cudaSuccess) cst = cudaGraphInstantiate(&g.exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (cst != cudaSuccess) {
+          dev_free(e, g.d_work);
+          return fail(e, SSE_ERR_CUDA, std::string("sweep-block graph capture: ") + cudaGetErrorString(cst));
+        }
         it = e->graphs.emplace(key, g).first;
       }
       CUDA_TRY(e, cudaEventRecord(e->ev0, e->stream));
@@ -775,7 +783,11 @@ int sse_engine_create(int32_t device, sse_engine **out) {
     delete e;
     return SSE_ERR_CUDA;
   }
-  cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaDeviceGetAttribute(&e->num_sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess ||
+      e->num_sms <= 0) {
+    delete e;
+    return SSE_ERR_CUDA;
+  }
   if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&e->ev0) != cudaSuccess || cudaEventCreate(&e->ev1) != cudaSuccess) {
     delete e;
