@@ -442,6 +442,28 @@ void dev_free(sse_engine *e, T *&p) {
   p = nullptr;
 }
 
+// Device buffers of one call, freed (stream-ordered) when the call returns, on every path.
+struct Scratch {
+  sse_engine *e;
+  std::vector<void **> held;
+  explicit Scratch(sse_engine *eng) : e(eng) {}
+  Scratch(const Scratch &) = delete;
+  Scratch &operator=(const Scratch &) = delete;
+  template <typename T>
+  int alloc(T **p, size_t count) {
+    const int rc = dev_alloc(e, p, count);
+    if (!rc) held.push_back(reinterpret_cast<void **>(p));
+    return rc;
+  }
+  ~Scratch() {
+    for (void **p : held)
+      if (*p) {
+        cudaFreeAsync(*p, e->stream);
+        *p = nullptr;
+      }
+  }
+};
+
 void clear_graphs(sse_engine *e) {
   for (auto &g : e->graphs) {
     if (g.second.exec) cudaGraphExecDestroy(g.second.exec);
@@ -709,13 +731,13 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
     }
     if (!grow.empty()) {
       GrowEntry *d_g = nullptr;
-      rc = dev_alloc(e, &d_g, grow.size());
+      Scratch scratch(e);
+      rc = scratch.alloc(&d_g, grow.size());
       if (rc) return rc;
       CUDA_TRY(e, cudaMemcpyAsync(d_g, grow.data(), sizeof(GrowEntry) * grow.size(), cudaMemcpyHostToDevice,
                                   e->stream));
       k_apply_growth<<<((int)grow.size() + 127) / 128, 128, 0, e->stream>>>(e->d_walkers, d_g, (int)grow.size());
       CUDA_TRY(e, cudaGetLastError());
-      dev_free(e, d_g);
       CUDA_TRY(e, cudaStreamSynchronize(e->stream));
     }
     work.swap(again);
@@ -1160,13 +1182,13 @@ int sse_sweep_each(sse_engine *e, int32_t count, const int32_t *ids, const int32
   int rc = ensure_work(e, (size_t)count);
   if (rc) return rc;
   int32_t *d_ns = nullptr;
-  rc = dev_alloc(e, &d_ns, (size_t)count);
+  Scratch scratch(e);
+  rc = scratch.alloc(&d_ns, (size_t)count);
   if (rc) return rc;
   CUDA_TRY(e, cudaMemcpyAsync(e->d_work, ids, sizeof(int32_t) * count, cudaMemcpyHostToDevice, e->stream));
   CUDA_TRY(e, cudaMemcpyAsync(d_ns, nsweeps, sizeof(int32_t) * count, cudaMemcpyHostToDevice, e->stream));
   k_set_targets<<<(count + 255) / 256, 256, 0, e->stream>>>(e->d_walkers, e->d_work, d_ns, count);
   CUDA_TRY(e, cudaGetLastError());
-  dev_free(e, d_ns);
   // targets are set: every pass keeps them (nsweeps = -1)
   return run_until_done(e, MODE_SWEEP, work, -1, flags);
 }
@@ -1185,11 +1207,12 @@ int sse_observables(sse_engine *e, int32_t count, const int32_t *ids, double *su
   int32_t *d_ids = nullptr, *d_off = nullptr;
   double *d_s = nullptr, *d_l = nullptr;
   long long *d_c = nullptr;
-  int rc = dev_alloc(e, &d_ids, count);
-  if (!rc) rc = dev_alloc(e, &d_off, count + 1);
-  if (!rc) rc = dev_alloc(e, &d_s, tot);
-  if (!rc) rc = dev_alloc(e, &d_l, tot);
-  if (!rc) rc = dev_alloc(e, &d_c, tot);
+  Scratch scratch(e);
+  int rc = scratch.alloc(&d_ids, count);
+  if (!rc) rc = scratch.alloc(&d_off, count + 1);
+  if (!rc) rc = scratch.alloc(&d_s, tot);
+  if (!rc) rc = scratch.alloc(&d_l, tot);
+  if (!rc) rc = scratch.alloc(&d_c, tot);
   if (rc) return rc;
   CUDA_TRY(e, cudaMemcpyAsync(d_ids, ids, sizeof(int32_t) * count, cudaMemcpyHostToDevice, e->stream));
   CUDA_TRY(e, cudaMemcpyAsync(d_off, off.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice, e->stream));
@@ -1198,11 +1221,6 @@ int sse_observables(sse_engine *e, int32_t count, const int32_t *ids, double *su
   CUDA_TRY(e, cudaMemcpyAsync(sums, d_s, sizeof(double) * tot, cudaMemcpyDeviceToHost, e->stream));
   CUDA_TRY(e, cudaMemcpyAsync(counts, d_c, sizeof(long long) * tot, cudaMemcpyDeviceToHost, e->stream));
   CUDA_TRY(e, cudaMemcpyAsync(last, d_l, sizeof(double) * tot, cudaMemcpyDeviceToHost, e->stream));
-  dev_free(e, d_ids);
-  dev_free(e, d_off);
-  dev_free(e, d_s);
-  dev_free(e, d_l);
-  dev_free(e, d_c);
   CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   return SSE_OK;
 }
@@ -1293,7 +1311,8 @@ int sse_vertex_list(sse_engine *e, int32_t id, int32_t *vertices, int32_t *v_fir
   if (rc) return rc;
   const int N = e->models[w.model].nsites;
   int32_t *d_vl = nullptr;
-  rc = dev_alloc(e, &d_vl, (size_t)N);
+  Scratch scratch(e);
+  rc = scratch.alloc(&d_vl, (size_t)N);
   if (rc) return rc;
   const size_t smem = (size_t)4 * N;
   CUDA_TRY(e, cudaFuncSetAttribute(k_link_debug, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1306,7 +1325,6 @@ int sse_vertex_list(sse_engine *e, int32_t id, int32_t *vertices, int32_t *v_fir
   CUDA_TRY(e, cudaMemcpyAsync(vf.data(), w.vfirst, sizeof(int32_t) * N, cudaMemcpyDeviceToHost, e->stream));
   if (w.n)
     CUDA_TRY(e, cudaMemcpyAsync(rec.data(), w.rec, sizeof(Rec) * (size_t)w.n, cudaMemcpyDeviceToHost, e->stream));
-  dev_free(e, d_vl);
   CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   auto conv = [&](int32_t x) { return x < 0 ? -1 : 4 * rec[x >> 2].slot + (x & 3); };
   if (vertices) {
@@ -1474,19 +1492,21 @@ int check_ladders(sse_engine *e, int32_t nladders, int32_t nrungs, const int32_t
 }
 
 struct PtBuffers {
+  Scratch scratch;
   int32_t *ids = nullptr, *accepted = nullptr;
   long long *acc = nullptr, *prop = nullptr;
   int *err = nullptr;
   size_t npairs = 0;
+  explicit PtBuffers(sse_engine *e) : scratch(e) {}
 };
 
 int pt_alloc(sse_engine *e, PtBuffers &b, int32_t nladders, int32_t nrungs, const int32_t *ids) {
   b.npairs = (size_t)nladders * (nrungs - 1);
-  int rc = dev_alloc(e, &b.ids, (size_t)nladders * nrungs);
-  if (!rc) rc = dev_alloc(e, &b.accepted, b.npairs);
-  if (!rc) rc = dev_alloc(e, &b.acc, b.npairs);
-  if (!rc) rc = dev_alloc(e, &b.prop, b.npairs);
-  if (!rc) rc = dev_alloc(e, &b.err, 1);
+  int rc = b.scratch.alloc(&b.ids, (size_t)nladders * nrungs);
+  if (!rc) rc = b.scratch.alloc(&b.accepted, b.npairs);
+  if (!rc) rc = b.scratch.alloc(&b.acc, b.npairs);
+  if (!rc) rc = b.scratch.alloc(&b.prop, b.npairs);
+  if (!rc) rc = b.scratch.alloc(&b.err, 1);
   if (rc) return rc;
   CUDA_TRY(e, cudaMemcpyAsync(b.ids, ids, sizeof(int32_t) * (size_t)nladders * nrungs, cudaMemcpyHostToDevice,
                               e->stream));
@@ -1494,14 +1514,6 @@ int pt_alloc(sse_engine *e, PtBuffers &b, int32_t nladders, int32_t nrungs, cons
   CUDA_TRY(e, cudaMemsetAsync(b.prop, 0, sizeof(long long) * b.npairs, e->stream));
   CUDA_TRY(e, cudaMemsetAsync(b.err, 0, sizeof(int), e->stream));
   return SSE_OK;
-}
-
-void pt_free(sse_engine *e, PtBuffers &b) {
-  dev_free(e, b.ids);
-  dev_free(e, b.accepted);
-  dev_free(e, b.acc);
-  dev_free(e, b.prop);
-  dev_free(e, b.err);
 }
 
 int pt_launch(sse_engine *e, PtBuffers &b, int32_t nladders, int32_t nrungs, uint64_t seed, uint64_t step) {
@@ -1532,7 +1544,7 @@ int sse_tempering_exchange(sse_engine *e, int32_t nladders, int32_t nrungs, cons
   if (rc || nladders == 0) return rc;
   cudaSetDevice(e->device);
   e->last_launches = 0;
-  PtBuffers b;
+  PtBuffers b(e);
   rc = pt_alloc(e, b, nladders, nrungs, ids);
   if (!rc) {
     CUDA_TRY(e, cudaEventRecord(e->ev0, e->stream));
@@ -1547,7 +1559,6 @@ int sse_tempering_exchange(sse_engine *e, int32_t nladders, int32_t nrungs, cons
     float ms = 0.0f;
     if (!rc && cudaEventElapsedTime(&ms, e->ev0, e->ev1) == cudaSuccess) e->last_ms = ms;
   }
-  pt_free(e, b);
   return rc;
 }
 
@@ -1559,12 +1570,9 @@ int sse_sweep_tempering(sse_engine *e, int32_t nladders, int32_t nrungs, const i
   int rc = check_ladders(e, nladders, nrungs, ids);
   if (rc || nladders == 0) return rc;
   cudaSetDevice(e->device);
-  PtBuffers b;
+  PtBuffers b(e);
   rc = pt_alloc(e, b, nladders, nrungs, ids);
-  if (rc) {
-    pt_free(e, b);
-    return rc;
-  }
+  if (rc) return rc;
   const std::vector<int32_t> work(ids, ids + (size_t)nladders * nrungs);
   double ms = 0.0;
   long long launches = 0;
@@ -1603,7 +1611,6 @@ int sse_sweep_tempering(sse_engine *e, int32_t nladders, int32_t nrungs, const i
                                   e->stream));
     CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   }
-  pt_free(e, b);
   e->last_ms = ms;
   e->last_launches = launches;
   if (rc) return rc;
