@@ -641,6 +641,15 @@ def main():
         work = np.array([(b["worm_steps"] - a["worm_steps"]) + (b["slot_visits"] - a["slot_visits"])
                          for a, b in zip(info0, info1)], dtype=float)
         phases = dict(zip(["diagonal", "link", "worm", "measure"], (cyc.sum(0) / cyc.sum()).round(4).tolist()))
+        worm_steps = sum(b["worm_steps"] - a["worm_steps"] for a, b in zip(info0, info1))
+        slots = sum(b["slot_visits"] - a["slot_visits"] for a, b in zip(info0, info1))
+        # what bounds the kernel: one dependent DRAM access per worm step, one warp per walker
+        latency = {"worm_cycles_per_step": float(cyc[:, 2].sum() / max(worm_steps, 1)),
+                   "diag_cycles_per_slot": float(cyc[:, 0].sum() / max(slots, 1)),
+                   "link_cycles_per_slot": float(cyc[:, 1].sum() / max(slots, 1)),
+                   "dram_pointer_chase_cycles": 790,
+                   "note": "per-walker SM clock cycles under full load; a lone dependent DRAM access costs about "
+                           "790 cycles on this GPU"}
         result = {
             "metric": METRIC,
             "value": value,
@@ -667,6 +676,7 @@ def main():
             },
             "operator_updates_per_s": opupd,
             "phase_cycle_share": phases,
+            "latency": latency,
             "load_balance_mean_over_max_walker_work": float(work.mean() / work.max()),
             "plain": {"value": plain_value, "unit": METRIC, "walkers": len(sub),
                       "path": "one kernel launch (one warp) per walker per sweep, synchronised after each"},
