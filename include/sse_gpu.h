@@ -46,7 +46,7 @@ typedef enum sse_status {
   SSE_ERR_TIMEOUT = 5,        /* a bounded device wait gave up */
   SSE_ERR_NOMEM = 6,          /* device or host allocation failed */
   SSE_ERR_STATE = 7,          /* call not valid in the walker's current state */
-  SSE_ERR_WORM_CAP = 8,       /* a worm exceeded the step cap (64 * (L + 16)) */
+  SSE_ERR_WORM_CAP = 8,       /* a worm exceeded the step cap (64 * (L + 16) unless set otherwise) */
   SSE_ERR_UNSUPPORTED = 9     /* model outside the engine's limits */
 } sse_status;
 
@@ -199,6 +199,13 @@ int sse_autotune_each(sse_engine *eng, int32_t count, const int32_t *ids, const 
 /* brackets a profiled region (cudaProfilerStart / cudaProfilerStop) for profilers started with
  * collection off; start != 0 opens the region, 0 closes it */
 int sse_profiler_range(sse_engine *eng, int32_t start);
+
+/* ---- worm step cap (no counterpart in the reference, whose worm_traverse! has no limit) ----
+ * A worm that has not closed after factor * (L + 16) steps stops its walker with SSE_ERR_WORM_CAP
+ * (the walker keeps that status; the other walkers go on).  The default factor is 64.  Some S >= 1
+ * vertex tables let worms enter cycles that never close; a smaller factor ends those sooner, at
+ * the price of stopping rare genuinely long worms. */
+int sse_walkers_set_worm_cap(sse_engine *eng, int32_t count, const int32_t *ids, int32_t factor);
 
 /* ---- parallel tempering between resident walkers (src/sse.jl:390-405) ----
  *

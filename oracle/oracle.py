@@ -93,6 +93,7 @@ class OrcWalker(C.Structure):
         ("obs_sum", P(C.c_double)),
         ("obs_last", P(C.c_double)),
         ("obs_count", P(C.c_int64)),
+        ("worm_cap_factor", C.c_int32),
     ]
 
 

@@ -124,6 +124,7 @@ orc_walker *orc_walker_create(const orc_model *m, double T, uint64_t seed, uint6
   w->avg_worm_length = 1.0;
   w->num_worms = init_num_worms;
   w->thermalization = thermalization;
+  w->worm_cap_factor = 64;
   w->state = (uint8_t *)calloc((size_t)m->nsites, 1);
   w->v_first = (int32_t *)malloc(sizeof(int32_t) * (size_t)m->nsites);
   w->v_last = (int32_t *)malloc(sizeof(int32_t) * (size_t)m->nsites);
@@ -310,7 +311,7 @@ static int64_t worm_traverse(const orc_model *m, orc_walker *w) {
   int32_t leg_in = l0, wormfunc = wormfunc0;
   int64_t p = p0;
   int64_t worm_length = 1;
-  const int64_t cap = 64 * (w->L + 16);
+  const int64_t cap = (int64_t)w->worm_cap_factor * (w->L + 16);
   for (;;) {
     uint32_t op = w->ops[p];
     uint32_t bond = op_bond(op);

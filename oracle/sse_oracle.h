@@ -92,6 +92,8 @@ typedef struct orc_walker {
   double *obs_sum;
   double *obs_last;
   int64_t *obs_count;
+  /* a worm stops the walker (ORC_ERR_WORM_CAP) after worm_cap_factor * (L + 16) steps; default 64 */
+  int32_t worm_cap_factor;
 } orc_walker;
 
 orc_walker *orc_walker_create(const orc_model *m, double T, uint64_t seed, uint64_t stream,

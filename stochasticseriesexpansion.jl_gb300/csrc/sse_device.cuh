@@ -118,7 +118,8 @@ struct DevWalker {
   long long init_cutoff, need_L;
   long long resize_after_therm, slot_visits, worm_steps;
   long long cyc[4];  // clock cycles spent in diagonal update, linking, worms, measurement
-  int32_t model, status, phase, warmup, warmup_done, pad;
+  int32_t model, status, phase, warmup, warmup_done;
+  int32_t cap_factor;  // a worm stops the walker after cap_factor * (L + 16) steps; 0: 64
 };
 
 // ---------------------------------------------------------------------------
@@ -746,11 +747,11 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
                                         Rec *__restrict__ rec, const int32_t *__restrict__ cidx,
                                         const int32_t *__restrict__ vfirst, uint8_t *__restrict__ state,
                                         unsigned long long *dbuf, bool thermalized, double &wlf, bool &have_wlf,
-                                        long long &steps, int lane, bool pf) {
+                                        long long &steps, int lane, bool pf, int cap_factor) {
   double total = 1.0;
   const double ceil_nw = ceil(wc.num_worms);
   const long long nworms = (long long)ceil_nw;
-  const long long cap = 64 * (c.L + 16);
+  const long long cap = (long long)(cap_factor > 0 ? cap_factor : 64) * (c.L + 16);
   const unsigned long long L = (unsigned long long)c.L;
   for (long long wi = 0; wi < nworms; wi++) {
     if (c.n == 0) continue;  // worm_traverse! returns 0 without drawing

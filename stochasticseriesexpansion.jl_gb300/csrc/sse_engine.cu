@@ -126,7 +126,7 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
         bool have_wlf = false;
         status = worm_update(M, c, wc, ops, wrec, W->cidx, W->vfirst, state,
                              reinterpret_cast<unsigned long long *>(smem), thermalized, wlf, have_wlf, worm_steps,
-                             lane, !staged);
+                             lane, !staged, W->cap_factor);
         if (status != ST_OK) break;
         if (have_wlf && lane == 0) observe(W, 5, wlf);
         sweeps++;
@@ -1456,6 +1456,19 @@ int sse_profiler_range(sse_engine *e, int32_t start) {
   cudaSetDevice(e->device);
   CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   CUDA_TRY(e, start ? cudaProfilerStart() : cudaProfilerStop());
+  return SSE_OK;
+}
+
+int sse_walkers_set_worm_cap(sse_engine *e, int32_t count, const int32_t *ids, int32_t factor) {
+  if (!e || (count && !ids)) return SSE_ERR_ARG;
+  if (factor < 1 || factor > (1 << 20)) return fail(e, SSE_ERR_ARG, "worm cap factor must be 1..2^20");
+  cudaSetDevice(e->device);
+  for (int i = 0; i < count; i++) {
+    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+    char *dst = reinterpret_cast<char *>(e->d_walkers + ids[i]) + offsetof(DevWalker, cap_factor);
+    CUDA_TRY(e, cudaMemcpyAsync(dst, &factor, sizeof(int32_t), cudaMemcpyHostToDevice, e->stream));
+  }
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   return SSE_OK;
 }
 

@@ -129,6 +129,7 @@ def lib():
             "sse_set_staging": ([eng, I32], C.c_int),
             "sse_get_staging": ([eng, P(I32)], C.c_int),
             "sse_walker_set_T": ([eng, I32, C.c_double], C.c_int),
+            "sse_walkers_set_worm_cap": ([eng, I32, P(I32), I32], C.c_int),
             "sse_tempering_exchange": ([eng, I32, I32, P(I32), C.c_uint64, C.c_uint64, P(I32)], C.c_int),
             "sse_sweep_tempering": ([eng, I32, I32, P(I32), I32, I32, C.c_uint64, C.c_uint64, U32, P(I64), P(I64)],
                                     C.c_int),
@@ -151,7 +152,7 @@ def exported_symbols():
         "sse_sweep", "sse_sweep_each", "sse_observables", "sse_walker_info_get", "sse_walker_export", "sse_walker_import",
         "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range", "sse_autotune",
         "sse_sweep_noalloc", "sse_walker_set_T", "sse_tempering_exchange", "sse_sweep_tempering",
-        "sse_set_staging", "sse_get_staging", "sse_autotune_each",
+        "sse_set_staging", "sse_get_staging", "sse_autotune_each", "sse_walkers_set_worm_cap",
     ]
 
 
@@ -375,6 +376,11 @@ class Engine:
 
     def profiler_range(self, start: bool):
         self._check(self._L.sse_profiler_range(self.h, int(bool(start))))
+
+    def set_worm_cap(self, ids, factor: int):
+        """Stop a walker when one of its worms exceeds factor * (L + 16) steps (default 64)."""
+        a, p = _ids(ids)
+        self._check(self._L.sse_walkers_set_worm_cap(self.h, len(a), p, int(factor)))
 
     def set_T(self, wid: int, T: float):
         """Carlo.parallel_tempering_change_parameter!(mc, :T, T) (src/sse.jl:399-405)."""

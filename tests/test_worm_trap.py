@@ -62,3 +62,48 @@ def test_engine_stops_trapped_walker_like_oracle(S, O):
     with pytest.raises(SSEError):
         eng.sweep(ids[:1], 1)
     eng.close()
+
+
+def test_oracle_smaller_cap_stops_sooner(S, O):
+    """A smaller cap factor ends the same trapped worm after fewer steps."""
+    flat = trap_model(S)
+    om = O.OracleModel(flat)
+    steps = {}
+    for factor in (64, 4):
+        w = O.OracleWalker(om, T=1 / TRAP["beta"], seed=TRAP["seed"], stream=TRAP["stream"],
+                           thermalization=TRAP["thermalization"])
+        w.w.worm_cap_factor = factor
+        w.init()
+        with pytest.raises(RuntimeError):
+            w.run(5, measure=False)
+        assert w.w.status == 8 and w.w.sweeps == TRAP["sweep"]
+        steps[factor] = w.w.worm_steps_total
+    assert steps[4] < steps[64]
+
+
+@pytest.mark.gpu
+def test_engine_worm_cap_factor_matches_oracle(S, O):
+    from sse_gb300.engine import Engine, SSEError
+
+    flat = trap_model(S)
+    eng = Engine(0)
+    mid = eng.register_model(flat)
+    ids = eng.create_walkers(mid, [dict(T=1 / TRAP["beta"], seed=TRAP["seed"], stream=TRAP["stream"],
+                                        thermalization=TRAP["thermalization"])])
+    eng.set_worm_cap(ids, 4)
+    eng.init(ids)
+    with pytest.raises(SSEError):
+        eng.sweep(ids, 5, measure=False)
+    om = O.OracleModel(flat)
+    w = O.OracleWalker(om, T=1 / TRAP["beta"], seed=TRAP["seed"], stream=TRAP["stream"],
+                       thermalization=TRAP["thermalization"])
+    w.w.worm_cap_factor = 4
+    w.init()
+    with pytest.raises(RuntimeError):
+        w.run(5, measure=False)
+    ops, st, inf = eng.export(int(ids[0]))
+    assert inf["status"] == 8 and inf["rng_counter"] == w.w.ctr and inf["worm_steps"] == w.w.worm_steps_total
+    assert np.array_equal(ops, w.ops)
+    with pytest.raises(SSEError):
+        eng.set_worm_cap(ids, 0)
+    eng.close()
