@@ -355,9 +355,6 @@ def run_other_workload(args):
         for m in sorted({m for m, _ in params}):
             ids += eng.create_walkers(m, [q for mm, q in params if mm == m]).tolist()
         ids = np.array(ids, dtype=np.int32)
-        # S=1 tables trap some worms in cycles that never close; for a throughput run stop those after
-        # 4 (L + 16) steps instead of the default 64 (L + 16), about 2 M instead of 34 M steps here
-        eng.set_worm_cap(ids, 4)
         eng.init(ids)
         failed = 0
         done = 0
@@ -380,7 +377,7 @@ def run_other_workload(args):
         Ls = np.array([info1[i]["L"] for i in ids.tolist()])
         line.update(config=desc, thermalization_sweeps=args.therm, thermalization_seconds=therm_s,
                     sweeps_per_step=args.sweeps_per_step, steps=args.steps, walker_sweeps_per_s=ws / t_dev,
-                    operator_updates_per_s=ou / t_dev, walkers_stopped_by_worm_cap=failed, worm_cap_factor=4,
+                    operator_updates_per_s=ou / t_dev, walkers_stopped_by_worm_cap=failed,
                     cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
     elif args.workload in ("magnet_bench", "cluster_bench"):
         line.update(run_reference_job(S, eng, args))
