@@ -368,6 +368,8 @@ struct HostModel {
   DevModel dev{};
   std::vector<void *> allocs;
   int32_t nsites = 0, nobs = 0;
+  // host copies used to validate imported walker state
+  std::vector<int32_t> bond_type, type_nverts, site_dims;
 };
 
 struct HostWalker {
@@ -914,6 +916,15 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
     if (d->site_dims[bi[b].x] != x.d0 || d->site_dims[bi[b].y] != x.d1)
       return fail(e, SSE_ERR_ARG, "site dimensions inconsistent with bond type dims");
   }
+  // every leg state is a valid state of its site (legs 0, 2 on the bond's first site, 1, 3 on the second)
+  for (int t = 0; t < d->ntypes; t++)
+    for (int v = 0; v < types[t].nverts; v++)
+      for (int l = 0; l < 4; l++)
+        if (d->leg_state[4 * ((size_t)types[t].vert_off + v) + l] >= ((l & 1) ? types[t].d1 : types[t].d0))
+          return fail(e, SSE_ERR_ARG, "leg state outside its site's dimension");
+  hm.bond_type.assign(d->bond_type, d->bond_type + d->nbonds);
+  hm.type_nverts.assign(d->type_nverts, d->type_nverts + d->ntypes);
+  hm.site_dims.assign(d->site_dims, d->site_dims + d->nsites);
   int rc = upload(e, hm, bi.data(), bi.size(), &m.bond_info);
   if (!rc) rc = upload(e, hm, d->site_dims, (size_t)d->nsites, &m.site_dims);
   if (!rc) rc = upload(e, hm, types.data(), types.size(), &m.types);
@@ -992,6 +1003,9 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
       return fail(e, SSE_ERR_ARG, "transition row outside the outcome table");
     const DevType &ty = types[row_type[i]];
     for (int o = start; o < start + cnt; o++) {
+      // the next step indexes this type's rows with the target vertex and the outgoing worm
+      if (((outc[o].packed >> 11) & 0x1FF) >= ty.nverts || ((outc[o].packed >> 2) & 0xFF) > ty.maxworm)
+        return fail(e, SSE_ERR_ARG, "transition outcome outside its bond type's tables");
       const int dim_out = (outc[o].packed & 1) ? ty.d1 : ty.d0;  // leg_out & 1: the bond's second site
       outc[o].packed = (outc[o].packed & 0xFFFFF) | (dim_out << 20);
     }
@@ -1279,11 +1293,13 @@ int sse_walker_import(sse_engine *e, int32_t id, const uint32_t *ops, const uint
     const uint32_t op = ops[p];
     if (!op) continue;
     n++;
-    if ((int)(op >> 11) >= hm.dev.nbonds || !(op & 1u)) return fail(e, SSE_ERR_ARG, "opstring has an invalid operator");
+    const int bond = (int)(op >> 11);
+    if (bond >= hm.dev.nbonds || !(op & 1u) || (int)((op >> 2) & 0x1FFu) >= hm.type_nverts[hm.bond_type[bond]])
+      return fail(e, SSE_ERR_ARG, "opstring has an invalid operator");
   }
   if (n != info->num_operators) return fail(e, SSE_ERR_ARG, "num_operators does not match the opstring");
   for (int i = 0; i < hm.nsites; i++)
-    if (state[i] >= 255) return fail(e, SSE_ERR_ARG, "bad spin state");
+    if ((int)state[i] >= hm.site_dims[i]) return fail(e, SSE_ERR_ARG, "spin state outside its site's dimension");
   int rc = grow_walker(e, id, std::max<long long>(info->L, 1));
   if (rc) return rc;
   DevWalker w;
@@ -1716,6 +1732,58 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
   __syncthreads();
   if (X->status != SSE_OK) {
     if (tid == 0) uw->status = X->status;
+    return;
+  }
+  // the contents the sweep indexes with: bonds, leg states, scatter outcomes and, for a walker that
+  // continues, its opstring and spin state (as sse_model_register and sse_walker_import check them)
+  __shared__ int s_bad;
+  if (tid == 0) s_bad = 0;
+  __syncthreads();
+  for (int b = tid; b < d.nbonds; b += nt) {
+    const int s0 = d.bond_sites[2 * b], s1 = d.bond_sites[2 * b + 1], t = d.bond_type[b];
+    if (s0 < 0 || s1 < 0 || s0 >= d.nsites || s1 >= d.nsites || s0 == s1 || t < 0 || t >= d.ntypes)
+      s_bad = 1;
+    else if (d.site_dims[s0] != d.type_dims[2 * t] || d.site_dims[s1] != d.type_dims[2 * t + 1])
+      s_bad = 1;
+  }
+  for (int t = 0; t < d.ntypes; t++)
+    for (int x = tid; x < 4 * d.type_nverts[t]; x += nt)
+      if (d.leg_state[4 * d.type_vert_off[t] + x] >= d.type_dims[2 * t + (x & 1)]) s_bad = 1;
+  for (int t = 0; t < d.ntypes; t++) {
+    const int r0 = d.type_trans_off[t], r1 = r0 + d.type_nverts[t] * 4 * d.type_maxworm[t];
+    for (int i = r0 + tid; i < r1; i += nt) {
+      const int st = d.trans_start[i];
+      if (st < 0) continue;
+      for (int o = st; o < st + d.trans_count[i]; o++)
+        if (d.out_leg[o] < 0 || d.out_leg[o] > 3 || d.out_worm[o] < 1 || d.out_worm[o] > d.type_maxworm[t] ||
+            d.out_target[o] < 0 || (d.out_target[o] >> 1) >= d.type_nverts[t])
+          s_bad = 1;
+    }
+  }
+  __syncthreads();
+  // the walker's own state, read only once the tables it indexes are known to be valid
+  if (!s_bad && uw->phase == PH_READY) {
+    const long long L = uw->L, n = uw->num_operators;
+    if (L < 0 || L > ops_capacity || n < 0 || n > L) {
+      s_bad = 1;
+    } else {
+      for (long long p = tid; p < L; p += nt) {
+        const uint32_t op = ops[p];
+        if (!op) continue;
+        const int bond = (int)(op >> 11);
+        if (bond >= d.nbonds || !(op & 1u) || (int)((op >> 2) & 0x1FFu) >= d.type_nverts[d.bond_type[bond]])
+          s_bad = 1;
+      }
+    }
+    for (int i = tid; i < d.nsites; i += nt)
+      if (state[i] >= d.site_dims[i]) s_bad = 1;
+  }
+  __syncthreads();
+  if (s_bad) {
+    if (tid == 0) {
+      X->status = SSE_ERR_ARG;
+      uw->status = SSE_ERR_ARG;
+    }
     return;
   }
   for (int t = tid; t < d.ntypes; t += nt) {
