@@ -200,6 +200,14 @@ int sse_autotune_each(sse_engine *eng, int32_t count, const int32_t *ids, const 
  * collection off; start != 0 opens the region, 0 closes it */
 int sse_profiler_range(sse_engine *eng, int32_t start);
 
+/* ---- invariant check (test/test_sse.jl:5-28, isconsistent) ----
+ * For each walker: propagating its spin state through its opstring, every operator's lower legs
+ * match the state they meet and the state after the last operator is the initial one (periodic
+ * imaginary time); every operator's bond and vertex exist; the operator count is num_operators.
+ * result[i]: 0 consistent, 1 sizes (L, num_operators, capacity), 2 invalid operator, 3 operator
+ * count, 4 leg state mismatch, 5 not periodic, 6 spin state outside its site's dimension. */
+int sse_check_walkers(sse_engine *eng, int32_t count, const int32_t *ids, int32_t *result);
+
 /* ---- worm step cap (no counterpart in the reference, whose worm_traverse! has no limit) ----
  * A worm that has not closed after factor * (L + 16) steps stops its walker with SSE_ERR_WORM_CAP
  * (the walker keeps that status; the other walkers go on).  The default factor is 64.  Some S >= 1

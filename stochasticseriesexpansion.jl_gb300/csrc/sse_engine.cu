@@ -262,6 +262,77 @@ __global__ void k_gather_obs(DevWalker *walkers, const int32_t *ids, int n, cons
 }
 
 // ---------------------------------------------------------------------------
+// invariant check (test/test_sse.jl:5-28, isconsistent): propagating the spin state through the
+// opstring, every operator's lower legs match the state it meets, and the state after the last
+// operator is the initial one again (periodic imaginary time).  Also checks the table ranges of
+// every operator and the operator count.  One warp per walker; lane 0 walks the opstring.
+// ---------------------------------------------------------------------------
+
+constexpr int CHK_OK = 0, CHK_SIZES = 1, CHK_OPERATOR = 2, CHK_COUNT = 3, CHK_LEGS = 4, CHK_PERIODIC = 5,
+              CHK_STATE = 6;
+
+__global__ void k_check(const DevModel *models, const DevWalker *walkers, const int32_t *ids, int n,
+                        int32_t *result, int smem_per_warp) {
+  extern __shared__ __align__(32) uint8_t smem[];
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  uint8_t *sst = smem + (size_t)(threadIdx.x >> 5) * smem_per_warp;
+  for (int i = warp; i < n; i += nwarps) {
+    const DevWalker &W = walkers[ids[i]];
+    const DevModel &M = models[W.model];
+    const int N = M.nsites;
+    int code = CHK_OK;
+    if (W.L < 0 || W.L > W.cap || W.n < 0 || W.n > W.L) code = CHK_SIZES;
+    bool bad_state = false;
+    for (int s = lane; s < N; s += 32) {
+      const uint8_t v = W.state[s];
+      bad_state |= v >= M.site_dims[s];
+      sst[s] = v;
+    }
+    if (__any_sync(FULL, bad_state) && code == CHK_OK) code = CHK_STATE;
+    __syncwarp();
+    if (lane == 0 && code == CHK_OK) {
+      long long count = 0;
+      for (long long p = 0; p < W.L && code == CHK_OK; p++) {
+        const uint32_t op = W.ops[p];
+        if (!op) continue;
+        count++;
+        const int bond = (int)(op >> 11);
+        if (!(op & 1u) || bond >= M.nbonds) {
+          code = CHK_OPERATOR;
+          break;
+        }
+        const int4 bi = M.bond_info[bond];
+        const DevType t = M.types[bi.z];
+        const int v = (int)((op >> 2) & 0x1FFu);
+        if (v >= t.nverts) {
+          code = CHK_OPERATOR;
+          break;
+        }
+        const uint8_t *ls = M.leg_state + 4 * (t.vert_off + v);
+        if (sst[bi.x] != ls[0] || sst[bi.y] != ls[1]) {
+          code = CHK_LEGS;
+          break;
+        }
+        sst[bi.x] = ls[2];
+        sst[bi.y] = ls[3];
+      }
+      if (code == CHK_OK && count != W.n) code = CHK_COUNT;
+      if (code == CHK_OK)
+        for (int s = 0; s < N; s++)
+          if (sst[s] != W.state[s]) {
+            code = CHK_PERIODIC;
+            break;
+          }
+    }
+    code = __shfl_sync(FULL, code, 0);
+    if (lane == 0) result[i] = code;
+    __syncwarp();
+  }
+}
+
+// ---------------------------------------------------------------------------
 // parallel tempering: Carlo.parallel_tempering_log_weight_ratio and
 // parallel_tempering_change_parameter! (src/sse.jl:390-405)
 // ---------------------------------------------------------------------------
@@ -1472,6 +1543,32 @@ int sse_profiler_range(sse_engine *e, int32_t start) {
   cudaSetDevice(e->device);
   CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   CUDA_TRY(e, start ? cudaProfilerStart() : cudaProfilerStop());
+  return SSE_OK;
+}
+
+int sse_check_walkers(sse_engine *e, int32_t count, const int32_t *ids, int32_t *result) {
+  if (!e || (count && (!ids || !result))) return SSE_ERR_ARG;
+  if (count == 0) return SSE_OK;
+  cudaSetDevice(e->device);
+  for (int i = 0; i < count; i++)
+    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+  const int max_ns = max_nsites_of(e, count, ids);
+  const int spw = (max_ns + 31) & ~31;
+  const int wpb = std::max(1, std::min(8, (int)((48 * 1024) / std::max(spw, 32))));
+  if ((size_t)wpb * spw > 227 * 1024) return fail(e, SSE_ERR_UNSUPPORTED, "too many sites for the check");
+  CUDA_TRY(e, cudaFuncSetAttribute(k_check, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)std::max<size_t>((size_t)wpb * spw, 48 * 1024)));
+  Scratch scratch(e);
+  int32_t *d_ids = nullptr, *d_res = nullptr;
+  int rc = scratch.alloc(&d_ids, (size_t)count);
+  if (!rc) rc = scratch.alloc(&d_res, (size_t)count);
+  if (rc) return rc;
+  CUDA_TRY(e, cudaMemcpyAsync(d_ids, ids, sizeof(int32_t) * count, cudaMemcpyHostToDevice, e->stream));
+  const int grid = (int)std::min<long long>((count + wpb - 1) / wpb, 8LL * e->num_sms);
+  k_check<<<grid, 32 * wpb, (size_t)wpb * spw, e->stream>>>(e->d_models, e->d_walkers, d_ids, count, d_res, spw);
+  CUDA_TRY(e, cudaGetLastError());
+  CUDA_TRY(e, cudaMemcpyAsync(result, d_res, sizeof(int32_t) * count, cudaMemcpyDeviceToHost, e->stream));
+  CUDA_TRY(e, cudaStreamSynchronize(e->stream));
   return SSE_OK;
 }
 

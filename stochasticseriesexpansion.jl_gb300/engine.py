@@ -130,6 +130,7 @@ def lib():
             "sse_get_staging": ([eng, P(I32)], C.c_int),
             "sse_walker_set_T": ([eng, I32, C.c_double], C.c_int),
             "sse_walkers_set_worm_cap": ([eng, I32, P(I32), I32], C.c_int),
+            "sse_check_walkers": ([eng, I32, P(I32), P(I32)], C.c_int),
             "sse_tempering_exchange": ([eng, I32, I32, P(I32), C.c_uint64, C.c_uint64, P(I32)], C.c_int),
             "sse_sweep_tempering": ([eng, I32, I32, P(I32), I32, I32, C.c_uint64, C.c_uint64, U32, P(I64), P(I64)],
                                     C.c_int),
@@ -153,6 +154,7 @@ def exported_symbols():
         "sse_vertex_list", "sse_last_timing", "sse_set_launch", "sse_get_launch", "sse_profiler_range", "sse_autotune",
         "sse_sweep_noalloc", "sse_walker_set_T", "sse_tempering_exchange", "sse_sweep_tempering",
         "sse_set_staging", "sse_get_staging", "sse_autotune_each", "sse_walkers_set_worm_cap",
+        "sse_check_walkers",
     ]
 
 
@@ -376,6 +378,15 @@ class Engine:
 
     def profiler_range(self, start: bool):
         self._check(self._L.sse_profiler_range(self.h, int(bool(start))))
+
+    def check(self, ids) -> np.ndarray:
+        """The reference's isconsistent invariant (plus periodicity, ranges and operator count) on the
+        device for every walker: 0 where consistent, else the failing check's code."""
+        a, p = _ids(ids)
+        out = np.zeros(len(a), dtype=np.int32)
+        if len(a):
+            self._check(self._L.sse_check_walkers(self.h, len(a), p, _p(out, C.c_int32)))
+        return out
 
     def set_worm_cap(self, ids, factor: int):
         """Stop a walker when one of its worms exceeds factor * (L + 16) steps (default 64)."""

@@ -3,7 +3,8 @@ beta = 16 in one batch, checked through properties that do not depend on the bat
 
 * sampled walkers equal the oracle bit for bit,
 * every sampled opstring is consistent with its spin state and periodic in imaginary time
-  (the reference's isconsistent, test/test_sse.jl:5-28),
+  (the reference's isconsistent, test/test_sse.jl:5-28), and every walker passes the same check
+  on the device,
 * every cutoff lies on the reference's growth ladder L <- floor(1.5 L + 100) from round(N T),
 * walkers re-run alone end in the same state as in the full batch.
 """
@@ -82,6 +83,13 @@ def test_fullsize_opstrings_consistent_and_on_growth_ladder(batch):
             off = 4 * (a["type_vert_off"][a["bond_type"][b]] + v)
             state[a["bond_sites"][2 * b: 2 * b + 2]] = a["leg_state"][off + 2: off + 4]
         assert np.array_equal(state, st)
+
+
+def test_fullsize_every_walker_passes_device_invariant_check(batch):
+    """isconsistent, periodicity, ranges and operator count for all 4096 walkers (sse_check_walkers)."""
+    eng, flat, mid, ids = batch
+    res = eng.check(ids)
+    assert res.shape == (NW,) and not res.any(), np.bincount(res)
 
 
 def test_fullsize_walkers_alone_equal_in_batch(batch):

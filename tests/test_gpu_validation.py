@@ -75,3 +75,24 @@ def test_import_rejects_bad_vertex_and_state(S, eng):
     eng.import_(int(wid), ops, st, inf)
     eng.sweep([wid], 2)
     assert eng.info(int(wid))["status"] == 0
+
+
+def test_device_check_finds_planted_inconsistency(S, eng):
+    """sse_check_walkers reports a spin flipped against the opstring (a valid state value, so
+    nothing is indexed out of range); the untouched walker passes."""
+    flat = square(S)
+    mid = eng.register_model(flat)
+    a, b = eng.create_walkers(mid, [dict(T=0.5, seed=2, stream=k) for k in range(2)])
+    eng.init([a, b])
+    eng.sweep([a, b], 4)
+    assert eng.check([a, b]).tolist() == [0, 0]
+    ops, st, inf = eng.export(int(b))
+    # flip a spin that an operator acts on
+    import sse_gb300.util as U
+
+    site = int(flat.arrays["bond_sites"][2 * U.dev_get_bond(int(ops[np.flatnonzero(ops)[0]]))])
+    st = st.copy()
+    st[site] ^= 1
+    eng.import_(int(b), ops, st, inf)
+    res = eng.check([a, b]).tolist()
+    assert res[0] == 0 and res[1] in (4, 5)
