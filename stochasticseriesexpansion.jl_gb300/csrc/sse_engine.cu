@@ -560,6 +560,17 @@ bool valid_id(sse_engine *e, int32_t id) {
   return id >= 0 && (size_t)id < e->walkers.size() && e->walkers[id].alive;
 }
 
+// The walkers of one launch: valid and distinct, so that no two warps ever run the same chain.
+int check_work_ids(sse_engine *e, int32_t count, const int32_t *ids) {
+  std::vector<char> seen(e->walkers.size(), 0);
+  for (int i = 0; i < count; i++) {
+    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+    if (seen[ids[i]]) return fail(e, SSE_ERR_ARG, "walker " + std::to_string(ids[i]) + " appears twice in one call");
+    seen[ids[i]] = 1;
+  }
+  return SSE_OK;
+}
+
 int ensure_work(sse_engine *e, size_t n) {
   if (n <= e->work_cap) return SSE_OK;
   size_t cap = std::max<size_t>(n, 2 * e->work_cap);
@@ -1223,18 +1234,18 @@ int sse_walkers_reserve(sse_engine *e, int32_t count, const int32_t *ids, int64_
 int sse_walkers_init(sse_engine *e, int32_t count, const int32_t *ids) {
   if (!e || (count && !ids)) return SSE_ERR_ARG;
   cudaSetDevice(e->device);
+  const int rc = check_work_ids(e, count, ids);
+  if (rc) return rc;
   std::vector<int32_t> work(ids, ids + count);
-  for (int32_t id : work)
-    if (!valid_id(e, id)) return fail(e, SSE_ERR_ARG, "unknown walker id");
   return run_until_done(e, MODE_INIT, work, 0, 0);
 }
 
 int sse_sweep(sse_engine *e, int32_t count, const int32_t *ids, int32_t nsweeps, uint32_t flags) {
   if (!e || (count && !ids) || nsweeps < 0) return SSE_ERR_ARG;
   cudaSetDevice(e->device);
+  const int crc = check_work_ids(e, count, ids);
+  if (crc) return crc;
   std::vector<int32_t> work(ids, ids + count);
-  for (int32_t id : work)
-    if (!valid_id(e, id)) return fail(e, SSE_ERR_ARG, "unknown walker id");
   if (flags & SSE_SWEEP_PLAIN) {
     // one launch per walker per sweep
     double ms = 0.0;
@@ -1258,11 +1269,11 @@ int sse_sweep_each(sse_engine *e, int32_t count, const int32_t *ids, const int32
   if (!e || (count && (!ids || !nsweeps))) return SSE_ERR_ARG;
   if (count == 0) return SSE_OK;
   cudaSetDevice(e->device);
+  const int crc = check_work_ids(e, count, ids);
+  if (crc) return crc;
   std::vector<int32_t> work(ids, ids + count);
-  for (int i = 0; i < count; i++) {
-    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+  for (int i = 0; i < count; i++)
     if (nsweeps[i] < 0) return fail(e, SSE_ERR_ARG, "negative sweep count");
-  }
   if (flags & SSE_SWEEP_PLAIN) return fail(e, SSE_ERR_ARG, "sse_sweep_each runs one batched launch");
   int rc = ensure_work(e, (size_t)count);
   if (rc) return rc;
@@ -1465,8 +1476,8 @@ int autotune_impl(sse_engine *e, int32_t count, const int32_t *ids, int32_t nswe
                   const int32_t *nsweeps_each, uint32_t flags, int32_t *best_warps_per_block,
                   int32_t *best_stage_bytes, double *best_ms) {
   if (!e || count <= 0 || !ids || (!nsweeps_each && nsweeps_probe <= 0)) return SSE_ERR_ARG;
-  for (int i = 0; i < count; i++)
-    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
+  const int crc = check_work_ids(e, count, ids);
+  if (crc) return crc;
   cudaSetDevice(e->device);
   // staging budgets: off, 8 and 32 KB, and room for the records of the 25th-percentile, median and
   // largest walker (25 % headroom for the operator count's fluctuations), where that fits an SM

@@ -96,3 +96,23 @@ def test_device_check_finds_planted_inconsistency(S, eng):
     eng.import_(int(b), ops, st, inf)
     res = eng.check([a, b]).tolist()
     assert res[0] == 0 and res[1] in (4, 5)
+
+
+def test_duplicate_walker_ids_rejected(S, eng):
+    """Two warps must never run the same chain: a walker listed twice is refused before any launch."""
+    from sse_gb300.engine import SSEError
+
+    mid = eng.register_model(square(S))
+    a, b = eng.create_walkers(mid, [dict(T=0.5, seed=3, stream=k) for k in range(2)])
+    with pytest.raises(SSEError):
+        eng.init([a, b, a])
+    eng.init([a, b])
+    with pytest.raises(SSEError):
+        eng.sweep([a, a], 1)
+    with pytest.raises(SSEError):
+        eng.sweep_each([b, a, b], [1, 1, 1])
+    with pytest.raises(SSEError):
+        eng.autotune([a, a], nsweeps_probe=1)
+    assert [eng.info(int(i))["sweeps"] for i in (a, b)] == [0, 0]
+    eng.sweep([a, b], 1)
+    assert eng.check([a, b]).tolist() == [0, 0]
