@@ -141,3 +141,27 @@ def test_request_fails_when_replacements_are_used_up(S):
     (res,) = loop.run([req], realtime=False)
     assert res.status == "SSE_ERR_WORM_CAP" and res.replaced == 0
     assert loop.summary()["failed"] == 1
+
+
+def test_cost_aware_ticks_give_small_walkers_more_sweeps(S):
+    """With tick_seconds every walker gets as many sweeps per tick as fit the tick at the estimated
+    rate, so a small model's walkers run many more sweeps per launch than a large model's."""
+    from sse_gb300.serving import Request, ServingLoop, projected_sweep_cost
+
+    eng = FakeEngine()
+    small = Request(0, 0.0, 0.5, "square", 4, 1.0, nwalkers=2, nsweeps=400, seed=1)
+    large = Request(1, 0.0, 1.0, "bilayer", 16, 8.0, nwalkers=2, nsweeps=400, seed=2)
+    loop = ServingLoop(eng, memory_budget=10**12, tick_seconds=0.25, walker_rate=1e6,
+                       clock=iter(np.arange(0, 1e6, 0.5)).__next__)
+    res = loop.run([small, large], realtime=False)
+    assert sorted(r.rid for r in res) == [0, 1]
+    ids, ns = eng.calls[0]
+    k_small, k_large = ns[0], ns[2]
+    c_small = projected_sweep_cost(0.5, "square", 4, 1.0)
+    c_large = projected_sweep_cost(1.0, "bilayer", 16, 8.0)
+    assert k_small == min(400, int(0.25 * 1e6 / c_small)) and k_large == max(1, int(0.25 * 1e6 / c_large))
+    assert k_small > k_large
+    # the rate estimate moved towards the measured one after the first tick
+    assert loop.rate != 1e6
+    for r in res:
+        assert np.all(r.sums[:, 0] == 400)
