@@ -1,9 +1,10 @@
 """Worms that never close.
 
-With S=1 Heisenberg tables many scatter rows have a single outcome (probability 1) in
-every optimal LP solution.  Deterministic rows can merge two worm paths, so a worm can
-enter a cycle of states that never reaches its tail.  The reference's worm_traverse!
-(src/sse.jl:262-303) has no length limit and would loop forever; the oracle and the
+With S=1 Heisenberg tables some worms wander without reaching their tail for far longer
+than any opstring length.  The tables satisfy detailed balance move by move, and the
+wandering worm keeps taking random scatter steps (it is not a deterministic cycle), so
+no early test can prove that it will never close.  The reference's worm_traverse!
+(src/sse.jl:262-303) has no length limit and would run on; the oracle and the
 engine stop the walker after 64 * (L + 16) steps with status 8 (worm cap).  This file
 pins one such walker on the CPU; the GPU test checks the engine stops it identically
 while the other walkers of its batch finish normally."""
