@@ -78,13 +78,13 @@ def test_request_draw_distribution(S):
     assert draw_requests(7, 5)[3] == draw_requests(7, 5)[3]
 
 
-class TrapEngine(FakeEngine):
-    """Stops the walker of stream `trap_stream` once, at its `trap_at`-th sweep, like a worm that never
-    closed (SSE_ERR_WORM_CAP)."""
+class CapStopEngine(FakeEngine):
+    """Stops the walker of stream `stop_stream` once, at its `stop_at`-th sweep, like a worm that ran
+    past the length cap (SSE_ERR_WORM_CAP)."""
 
-    def __init__(self, trap_stream, trap_at):
+    def __init__(self, stop_stream, stop_at):
         super().__init__()
-        self.trap_stream, self.trap_at = trap_stream, trap_at
+        self.stop_stream, self.stop_at = stop_stream, stop_at
         self.status = {}
 
     def sweep_each(self, ids, ns, measure=True):
@@ -96,8 +96,8 @@ class TrapEngine(FakeEngine):
             w = self.walkers[i]
             if self.status.get(i, 0):
                 continue
-            if w["p"]["stream"] == self.trap_stream and w["sweeps"] < self.trap_at <= w["sweeps"] + n:
-                w["sweeps"] = self.trap_at
+            if w["p"]["stream"] == self.stop_stream and w["sweeps"] < self.stop_at <= w["sweeps"] + n:
+                w["sweeps"] = self.stop_at
                 self.status[i] = 8
                 hit = True
             else:
@@ -118,7 +118,7 @@ class TrapEngine(FakeEngine):
 def test_stopped_walker_is_replaced_by_a_fresh_chain(S):
     from sse_gb300.serving import Request, ServingLoop
 
-    eng = TrapEngine(trap_stream=1, trap_at=17)
+    eng = CapStopEngine(stop_stream=1, stop_at=17)
     req = Request(0, 0.0, 1.0, "square", 4, 1.0, nwalkers=3, nsweeps=40, seed=5)
     loop = ServingLoop(eng, memory_budget=10**12, tick_sweeps=10, clock=iter(np.arange(0, 1e6, 0.5)).__next__)
     (res,) = loop.run([req], realtime=False)
@@ -134,7 +134,7 @@ def test_stopped_walker_is_replaced_by_a_fresh_chain(S):
 def test_request_fails_when_replacements_are_used_up(S):
     from sse_gb300.serving import Request, ServingLoop
 
-    eng = TrapEngine(trap_stream=0, trap_at=3)
+    eng = CapStopEngine(stop_stream=0, stop_at=3)
     req = Request(0, 0.0, 1.0, "square", 4, 1.0, nwalkers=2, nsweeps=20, seed=5)
     loop = ServingLoop(eng, memory_budget=10**12, tick_sweeps=10, retries=0,
                        clock=iter(np.arange(0, 1e6, 0.5)).__next__)
