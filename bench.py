@@ -456,7 +456,7 @@ def run_uneven_balanced(S, eng, args, rng):
 
 
 def reference_job_model(S, name):
-    """The benchmark tasks of the reference's test/test_jobs.jl:113-165, timed there by
+    """The benchmark tasks of the reference's test/test_jobs.jl:113-167, timed there by
     test/benchmarks.jl:20-40 (one task: 2000 thermalisation + 5000 measured sweeps)."""
     if name == "magnet_bench":
         p = {"lattice": {"unitcell": S.UnitCells.square, "size": (10, 10)}, "J": 1.23, "hz": -0.2,

@@ -56,7 +56,7 @@ typedef struct sse_engine sse_engine;
  * Flat model tables (the SSEData of src/sse_data.jl with its VertexData of
  * src/vertex_data.jl:13-28, plus the magnetisation-estimator coefficients).
  * Replaces the reference's `generate_sse_data(model)` output
- * (src/abstract_model.jl:280, src/models/magnet/magnet.jl:169-184).
+ * (src/abstract_model.jl:31-40, src/models/magnet/magnet.jl:169-184).
  * All arrays are copied to the device by sse_model_register.
  * Limits: two-site bonds only (leg count 4), < 2^21 bonds, <= 512 vertices
  * per bond type, site dimension <= 255.

@@ -59,7 +59,7 @@ def _dimer_basis() -> ClusterBasis:
 
 
 class ClusterBases:
-    """Predefined cluster bases (cluster.jl:309-323)."""
+    """Predefined cluster bases (cluster.jl:308-323)."""
 
     dimer = _dimer_basis()
 
@@ -67,7 +67,7 @@ class ClusterBases:
 def lift_twobody_operator(op, site_dims, sites) -> np.ndarray:
     """Embed a two-site operator ``op`` (on the kron product of sites[0], sites[1], in that order) into
     the product space of ``site_dims`` (first factor slowest, as kron), acting as the identity on the
-    other factors (cluster.jl:85-124).  ``sites`` are 1-based."""
+    other factors (cluster.jl:79-126).  ``sites`` are 1-based."""
     site_dims = tuple(int(d) for d in site_dims)
     a, b = sites[0] - 1, sites[1] - 1
     if a == b:
@@ -91,7 +91,7 @@ def lift_twobody_operator(op, site_dims, sites) -> np.ndarray:
 
 
 def build_cluster_hamiltonians(cluster_ids, uc_bonds, bond_params, site_spin_states):
-    """cluster.jl:126-199.  ``cluster_ids``: 1-based id of each unit-cell site; ``bond_params``: the
+    """cluster.jl:128-196.  ``cluster_ids``: 1-based id of each unit-cell site; ``bond_params``: the
     first cell's bond parameters in unit-cell bond order.  Returns the intra-cluster Hamiltonian of
     every cluster id and a dict (iuc, juc, jd) -> inter-cluster bond Hamiltonian, in first-appearance
     order of the unit-cell bonds."""
@@ -126,7 +126,7 @@ def build_cluster_hamiltonians(cluster_ids, uc_bonds, bond_params, site_spin_sta
 
 
 def absorb_intracluster_hamiltonians(intra, inter):
-    """cluster.jl:201-224: every inter-cluster bond type takes 1/coordination of the intra-cluster
+    """cluster.jl:198-220: every inter-cluster bond type takes 1/coordination of the intra-cluster
     Hamiltonian of each of its two clusters (coordination counted over bond types)."""
     coord = [sum((k[0] == c) + (k[1] == c) for k in inter) for c in range(1, len(intra) + 1)]
     out = {}
@@ -138,7 +138,7 @@ def absorb_intracluster_hamiltonians(intra, inter):
 
 
 class ClusterModel(AbstractModel):
-    """cluster.jl:27-63."""
+    """cluster.jl:26-62."""
 
     def __init__(self, params: dict):
         inner = params["inner_model"](params)
@@ -181,18 +181,18 @@ class ClusterModel(AbstractModel):
         return self.opstring_estimators
 
     def magnetization_state(self, site_idx: int, state_idx: int, quantum_number: int = 1) -> float:
-        """cluster.jl:67-74: quantum number ``quantum_number`` (1-based) of basis state ``state_idx`` of
+        """cluster.jl:66-73: quantum number ``quantum_number`` (1-based) of basis state ``state_idx`` of
         the cluster at SSE site ``site_idx``."""
         nuc_clusters = len(self.basis)
         cid = (site_idx - 1) % nuc_clusters + 1
         return float(self.basis[cid - 1].quantum_numbers[state_idx - 1][quantum_number - 1])
 
     def staggered_sign(self, spec, site_idx: int) -> int:
-        """cluster.jl:76."""
+        """cluster.jl:75."""
         return 1
 
     def generate_sse_data(self) -> SSEData:
-        """cluster.jl:241-306: the inter-cluster bonds of the lattice, duplicates merged, with one
+        """cluster.jl:242-306: the inter-cluster bonds of the lattice, duplicates merged, with one
         vertex table per bond type from U' H U, U = kron of the two cluster transformations."""
         mag = self.inner_model
         lat = mag.lattice

@@ -39,7 +39,7 @@ class MagnetizationEstimatorSpec:
     ordering_vector: tuple
     stagger_uc: bool
     prefix: str
-    tag: int | None = None  # quantum-number index for cluster models (cluster.jl:226-239)
+    tag: int | None = None  # quantum-number index for cluster models (cluster.jl:222-240)
 
 
 def magnetization_estimator_standard_prefix(q, stagger_uc: bool) -> str:

@@ -49,7 +49,7 @@ def hamiltonian(S, model):
 
 
 def ed_observables(S, model, Ts):
-    """test/ed/ed.jl:376-412 and test/ed/magnet.jl:439-497."""
+    """test/ed/ed.jl:49-72 and 121-157 (ensemble averages, energy and specific heat) and test/ed/magnet.jl:27-97 (magnetisation estimators)."""
     H, lif = hamiltonian(S, model)
     Es, psi = np.linalg.eigh(H)
     Ts = np.asarray(Ts, dtype=float)

@@ -1,5 +1,5 @@
 """ClusterModel (src/models/cluster/cluster.jl): ports of test/models/test_cluster.jl, and the
-oracle against exact diagonalisation on the reference's cluster ED job (test/test_jobs.jl:70-110)."""
+oracle against exact diagonalisation on the reference's cluster ED job (test/test_jobs.jl:69-110)."""
 
 import numpy as np
 import pytest
@@ -21,7 +21,7 @@ def dimer_magnet_params(S):
 
 
 def cluster_job_params(S):
-    """The cluster ED job, test/test_jobs.jl:70-104."""
+    """The cluster ED job, test/test_jobs.jl:69-110."""
     return {
         "inner_model": S.MagnetModel,
         "lattice": {"unitcell": S.UnitCells.fully_frust_square_bilayer, "size": (2, 2)},
@@ -95,7 +95,7 @@ def test_cluster_basis_count_checked(S):
 
 def test_cluster_quantum_number_estimator_coefficients(S):
     """magnetization_state of a cluster model is the chosen quantum number of the basis state
-    (cluster.jl:67-74); with the dimer's m the estimator measures the total S^z."""
+    (cluster.jl:66-73); with the dimer's m the estimator measures the total S^z."""
     model = S.ClusterModel(cluster_job_params(S))
     flat = S.flatten_model(model)
     assert flat.est_prefixes == [""] and flat.maxdim == 4

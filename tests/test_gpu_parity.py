@@ -40,7 +40,7 @@ def bilayer_s1(S, L=4):
 
 
 def cluster_dimer(S):
-    """The reference's cluster ED job (test/test_jobs.jl:70-104): dims-4 dimer sites, signed tables."""
+    """The reference's cluster ED job (test/test_jobs.jl:69-110): dims-4 dimer sites, signed tables."""
     return S.ClusterModel({
         "inner_model": S.MagnetModel,
         "lattice": {"unitcell": S.UnitCells.fully_frust_square_bilayer, "size": (3, 2)},

@@ -107,7 +107,7 @@ def isconsistent(flat, ops, state0):
 
 
 def test_sse_mc_consistency_mixed_spins(S, O):
-    # test/test_sse.jl:295-326: honeycomb 4x4 with S=1/2 and S=1 sublattices, T=0.1
+    # test/test_sse.jl:63-94: honeycomb 4x4 with S=1/2 and S=1 sublattices, T=0.1
     params = {"T": 0.1, "measure": [], "parameter_map": {"S": ("S1", "S2")},
               "lattice": {"unitcell": S.UnitCells.honeycomb, "size": (4, 4)}, "J": 1.4, "S1": 0.5, "S2": 1.0}
     m = S.MagnetModel(params)
@@ -123,7 +123,7 @@ def test_sse_mc_consistency_mixed_spins(S, O):
 
 
 def test_worm_traverse_tiny_opstrings(S, O):
-    # test/test_sse.jl:262-292: single worms on hand-built opstrings stay consistent
+    # test/test_sse.jl:30-61: single worms on hand-built opstrings stay consistent
     m = S.MagnetModel({"lattice": {"unitcell": S.UnitCells.square, "size": (4, 4)}, "J": 1.0})
     flat = S.flatten_model(m)
     om = O.OracleModel(flat)

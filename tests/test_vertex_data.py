@@ -38,7 +38,7 @@ def heisenberg_bond(S):
 
 
 def test_vertex_apply_change_inverse(S):
-    # test/test_vertex_data.jl:93-109
+    # test/test_vertex_data.jl:63-79
     from sse_gb300.vertex_data import vertex_apply_change
     import itertools
 
@@ -52,7 +52,7 @@ def test_vertex_apply_change_inverse(S):
 
 
 def test_s12_heisenberg_known_answers(S):
-    # test/test_vertex_data.jl:111-130
+    # test/test_vertex_data.jl:81-100
     import sse_gb300.util as U
 
     vd = S.make_vertex_data((2, 2), heisenberg_bond(S), energy_offset_factor=0.0)
@@ -69,7 +69,7 @@ def test_s12_heisenberg_known_answers(S):
 
 @pytest.mark.parametrize("dims", [(4, 4), (2, 4)])
 def test_random_hamiltonian(S, dims):
-    # test/test_vertex_data.jl:132-166
+    # test/test_vertex_data.jl:102-135
     rng = np.random.default_rng(11)
     H = rng.random((int(np.prod(dims)), int(np.prod(dims))))
     vd = S.make_vertex_data(dims, H)
