@@ -282,7 +282,7 @@ def run_reference(args):
 
 
 def sweep_tolerant(eng, ids, nsweeps, measure=True, graph=False):
-    """sse_sweep over a batch; walkers stopped by an error (a worm that never closed) are dropped
+    """sse_sweep over a batch; walkers stopped by an error (a worm past the step cap) are dropped
     from the batch and counted, the others continue."""
     from sse_gb300.engine import SSEError
 

@@ -210,9 +210,12 @@ int sse_check_walkers(sse_engine *eng, int32_t count, const int32_t *ids, int32_
 
 /* ---- worm step cap (no counterpart in the reference, whose worm_traverse! has no limit) ----
  * A worm that has not closed after factor * (L + 16) steps stops its walker with SSE_ERR_WORM_CAP
- * (the walker keeps that status; the other walkers go on).  The default factor is 64.  Some S >= 1
- * vertex tables let worms enter cycles that never close; a smaller factor ends those sooner, at
- * the price of stopping rare genuinely long worms. */
+ * (the walker keeps that status; the other walkers go on).  The default factor is 64.  With S >= 1
+ * and cluster-basis vertex tables, worms of the first thermalisation sweeps (while L is still
+ * small) can run for orders of magnitude longer than the opstring before they close, over 10^9
+ * steps in some chains; the cap bounds how long one walker holds up its batch.  After
+ * thermalisation worms rarely pass 64 * (L + 16) steps.  A smaller factor stops such walkers
+ * sooner and stops more of them. */
 int sse_walkers_set_worm_cap(sse_engine *eng, int32_t count, const int32_t *ids, int32_t factor);
 
 /* ---- parallel tempering between resident walkers (src/sse.jl:390-405) ----

@@ -95,7 +95,7 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
     if (phase != PH_READY) {
       status = ST_STATE;
     } else if (W->status != ST_OK && W->status != ST_NEED_GROW) {
-      // a walker stopped by an error (e.g. a worm that never closed) keeps its status: its
+      // a walker stopped by an error (e.g. a worm past the step cap) keeps its status: its
       // opstring was left mid-update and must not be swept again
       status = W->status;
     } else {

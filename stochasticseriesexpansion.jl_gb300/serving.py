@@ -13,7 +13,7 @@ unmeasured).  The loop
   arrive while others run join the next launch,
 * retires a request as soon as its walkers are done, reporting its
   observables and its time-to-result (completion - arrival),
-* replaces a walker that the engine stopped (a worm that never closed,
+* replaces a walker that the engine stopped (a worm past the step cap,
   SSE_ERR_WORM_CAP) with a fresh chain, up to `retries` times per walker:
   slot k of a request runs stream k, its a-th replacement stream
   k + a * nwalkers, each replacement all of the request's sweeps from

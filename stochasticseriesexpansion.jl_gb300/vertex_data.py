@@ -165,10 +165,10 @@ def _solve_lp(cost, A, b, lp_tolerance, lp_point):
     lp_point = "vertex": a basic optimal solution (HiGHS simplex, like the reference's solver).
     lp_point = "central": a point inside the optimal face (HiGHS interior point without
     crossover), polished onto A x = b on its support.  The optimum is not unique for S >= 1;
-    vertex solutions put probability 1 on many single outcomes, and such deterministic
-    transitions can merge two worm paths into a cycle that never reaches the worm's tail (a
-    worm that never closes).  A central optimum keeps every transition that some optimal
-    solution allows, with the same (minimal) bounce weight.
+    vertex solutions put probability 1 on many single outcomes.  A central optimum keeps every
+    transition that some optimal solution allows, with the same (minimal) bounce weight.  With
+    central tables no walker ran a worm past the step cap in sampled dimer-basis and S=1
+    square-lattice runs; S=1 bilayer walkers still did, and mixed-spin honeycomb walkers began to.
     """
     import warnings as _w
 
