@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define SSE_GPU_ABI_VERSION 2
+#define SSE_GPU_ABI_VERSION 3
 
 typedef enum sse_status {
   SSE_OK = 0,
@@ -116,6 +116,7 @@ typedef struct sse_walker_info {
   int64_t slot_visits;   /* diagonal-update slot visits, cumulative */
   int64_t worm_steps;    /* worm vertex visits (scatter calls), cumulative */
   int64_t phase_cycles[4]; /* SM clock cycles in diagonal update, linking, worm update, measurement */
+  int64_t worm_undos;    /* thermalisation sweeps whose worm phase was undone at the worm step cap */
 } sse_walker_info;
 
 /* sse_sweep flags */
@@ -209,13 +210,18 @@ int sse_profiler_range(sse_engine *eng, int32_t start);
 int sse_check_walkers(sse_engine *eng, int32_t count, const int32_t *ids, int32_t *result);
 
 /* ---- worm step cap (no counterpart in the reference, whose worm_traverse! has no limit) ----
- * A worm that has not closed after factor * (L + 16) steps stops its walker with SSE_ERR_WORM_CAP
- * (the walker keeps that status; the other walkers go on).  The default factor is 64.  With S >= 1
- * and cluster-basis vertex tables, worms of the first thermalisation sweeps (while L is still
- * small) can run for orders of magnitude longer than the opstring before they close, over 10^9
- * steps in some chains; the cap bounds how long one walker holds up its batch.  After
- * thermalisation worms rarely pass 64 * (L + 16) steps.  A smaller factor stops such walkers
- * sooner and stops more of them. */
+ * A worm that has not closed after factor * (L + 16) steps
+ *  - in a thermalisation sweep (sweeps <= thermalization) undoes the sweep's worm phase: the
+ *    opstring returns to its state after the diagonal update, the worm-count controller and the
+ *    spin state stay as they were, the draws the worms consumed stay consumed, worm_undos counts
+ *    it, and the walker goes on (thermalisation sweeps need no detailed balance);
+ *  - in a measured sweep stops its walker with SSE_ERR_WORM_CAP (the walker keeps that status;
+ *    the other walkers go on).
+ * The default factor is 64.  With S >= 1 and cluster-basis vertex tables, worms of the first
+ * thermalisation sweeps (while L is still small) can run for orders of magnitude longer than the
+ * opstring before they close, over 10^9 steps in some chains; the cap bounds how long one walker
+ * holds up its batch.  After thermalisation worms rarely pass 64 * (L + 16) steps.  A smaller
+ * factor undoes or stops such worms sooner and more often. */
 int sse_walkers_set_worm_cap(sse_engine *eng, int32_t count, const int32_t *ids, int32_t factor);
 
 /* ---- parallel tempering between resident walkers (src/sse.jl:390-405) ----
@@ -303,6 +309,7 @@ typedef struct sse_noalloc_walker {
   int64_t need_capacity; /* with SSE_ERR_CAPACITY: opstring slots the walker needs next */
   int64_t slot_visits;
   int64_t worm_steps;
+  int64_t worm_undos;    /* thermalisation worm phases undone at the worm step cap */
 } sse_noalloc_walker;
 
 /* Runs Carlo.init! (when walker->phase == 0) and then nsweeps Carlo steps of one walker,

@@ -94,6 +94,9 @@ class OrcWalker(C.Structure):
         ("obs_last", P(C.c_double)),
         ("obs_count", P(C.c_int64)),
         ("worm_cap_factor", C.c_int32),
+        ("worm_undos", C.c_int64),
+        ("ops_saved", P(C.c_uint32)),
+        ("ops_saved_cap", C.c_int64),
     ]
 
 

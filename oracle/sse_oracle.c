@@ -142,6 +142,7 @@ orc_walker *orc_walker_create(const orc_model *m, double T, uint64_t seed, uint6
 void orc_walker_destroy(orc_walker *w) {
   if (!w) return;
   free(w->ops);
+  free(w->ops_saved);
   free(w->state);
   free(w->vertices);
   free(w->v_first);
@@ -359,8 +360,24 @@ static int64_t worm_traverse(const orc_model *m, orc_walker *w) {
 int orc_worm_update(const orc_model *m, orc_walker *w, int32_t thermalized) {
   double total_worm_length = 1.0;
   int64_t nworms = (int64_t)ceil(w->num_worms);
+  /* thermalisation: keep the opstring of the diagonal update, to undo the worm phase at the cap */
+  if (!thermalized && nworms > 0 && w->num_operators > 0) {
+    if (w->L > w->ops_saved_cap) {
+      uint32_t *p = (uint32_t *)realloc(w->ops_saved, sizeof(uint32_t) * (size_t)w->ops_cap);
+      if (!p) return w->status = ORC_ERR_NOMEM;
+      w->ops_saved = p;
+      w->ops_saved_cap = w->ops_cap;
+    }
+    memcpy(w->ops_saved, w->ops, sizeof(uint32_t) * (size_t)w->L);
+  }
   for (int64_t i = 0; i < nworms; i++) {
     int64_t len = worm_traverse(m, w);
+    if (len < 0 && w->status == ORC_ERR_WORM_CAP && !thermalized) {
+      memcpy(w->ops, w->ops_saved, sizeof(uint32_t) * (size_t)w->L);
+      w->status = ORC_OK;
+      w->worm_undos++;
+      return ORC_OK;
+    }
     if (len < 0) return w->status;
     total_worm_length += (double)len;
   }

@@ -29,6 +29,9 @@ constexpr int ST_INVALID_VERTEX = 4;
 constexpr int ST_TIMEOUT = 5;
 constexpr int ST_STATE = 7;
 constexpr int ST_WORM_CAP = 8;
+// worm_update only: a thermalisation worm passed the step cap and the sweep's worm phase was
+// undone; the caller counts it and carries on with ST_OK (never stored in a walker)
+constexpr int ST_WORM_UNDONE = -8;
 constexpr int ST_NEED_GROW = 100;
 
 // walker phases
@@ -117,6 +120,7 @@ struct DevWalker {
   long long therm, sweeps, target;
   long long init_cutoff, need_L;
   long long resize_after_therm, slot_visits, worm_steps;
+  long long worm_undos;  // thermalisation worm phases undone at the step cap
   long long cyc[4];  // clock cycles spent in diagonal update, linking, worms, measurement
   int32_t model, status, phase, warmup, warmup_done;
   int32_t cap_factor;  // a worm stops the walker after cap_factor * (L + 16) steps; 0: 64
@@ -815,6 +819,12 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
     steps += (long long)(ctr - c.ctr);  // one draw per scatter
     c.ctr = ctr;
     const long long len = shfl_ll(cs.len, 0);
+    if (status == ST_WORM_CAP && !thermalized) {
+      // undo the worm phase: the worms rewrote only the records, so ops[] still holds the
+      // opstring of the diagonal update; the controller and the spin state stay as they were
+      // and the draws the worms consumed stay consumed
+      return ST_WORM_UNDONE;
+    }
     if (status != ST_OK) {
       for (long long k = lane; k < c.n; k += 32) {
         const int2 os = reinterpret_cast<const int2 *>(rec + k)[2];

@@ -127,6 +127,10 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
         status = worm_update(M, c, wc, ops, wrec, W->cidx, W->vfirst, state,
                              reinterpret_cast<unsigned long long *>(smem), thermalized, wlf, have_wlf, worm_steps,
                              lane, !staged, W->cap_factor);
+        if (status == ST_WORM_UNDONE) {  // rare: counted straight in the walker record
+          status = ST_OK;
+          if (lane == 0) W->worm_undos++;
+        }
         if (status != ST_OK) break;
         if (have_wlf && lane == 0) observe(W, 5, wlf);
         sweeps++;
@@ -1335,6 +1339,7 @@ static void info_from(const DevWalker &w, sse_walker_info *info) {
   info->resize_after_thermalization = w.resize_after_therm;
   info->slot_visits = w.slot_visits;
   info->worm_steps = w.worm_steps;
+  info->worm_undos = w.worm_undos;
   for (int i = 0; i < 4; i++) info->phase_cycles[i] = w.cyc[i];
 }
 
@@ -2008,6 +2013,7 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
     w.init_cutoff = cut;
     w.slot_visits = uw->slot_visits;
     w.worm_steps = uw->worm_steps;
+    w.worm_undos = uw->worm_undos;
     w.model = 0;
     w.phase = uw->phase == PH_READY ? PH_READY : (uw->phase == PH_WARMUP ? PH_WARMUP : PH_NEW);
     w.warmup = uw->diagonal_warmup_sweeps;
@@ -2034,6 +2040,7 @@ __global__ void k_noalloc_finish(NoAllocScratch *X, sse_noalloc_walker *uw) {
   uw->warmup_done = w.warmup_done;
   uw->slot_visits = w.slot_visits;
   uw->worm_steps = w.worm_steps;
+  uw->worm_undos = w.worm_undos;
   int st = w.status;
   if (st == ST_NEED_GROW) {
     st = SSE_ERR_CAPACITY;

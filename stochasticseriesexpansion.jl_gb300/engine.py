@@ -13,6 +13,9 @@ import numpy as np
 
 from .build import LIB
 
+# SSE_GPU_ABI_VERSION of include/sse_gpu.h whose structs these bindings mirror
+ABI_VERSION = 3
+
 P = C.POINTER
 
 SSE_SWEEP_MEASURE = 1
@@ -69,6 +72,7 @@ class WalkerInfo(C.Structure):
         ("rng_counter", C.c_uint64), ("num_worms", C.c_double), ("avg_worm_length", C.c_double), ("T", C.c_double),
         ("status", C.c_int32), ("model", C.c_int32), ("resize_after_thermalization", C.c_int64),
         ("slot_visits", C.c_int64), ("worm_steps", C.c_int64), ("phase_cycles", C.c_int64 * 4),
+        ("worm_undos", C.c_int64),
     ]
 
     def as_dict(self):
@@ -87,7 +91,7 @@ class NoAllocWalker(C.Structure):
         ("thermalization", C.c_int64), ("L", C.c_int64), ("num_operators", C.c_int64), ("sweeps", C.c_int64),
         ("rng_counter", C.c_uint64), ("num_worms", C.c_double), ("avg_worm_length", C.c_double),
         ("warmup_done", C.c_int32), ("status", C.c_int32), ("need_capacity", C.c_int64),
-        ("slot_visits", C.c_int64), ("worm_steps", C.c_int64),
+        ("slot_visits", C.c_int64), ("worm_steps", C.c_int64), ("worm_undos", C.c_int64),
     ]
 
 
@@ -141,6 +145,9 @@ def lib():
             f = getattr(L, name)
             f.argtypes = args
             f.restype = res
+        if L.sse_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{LIB} has ABI version {L.sse_abi_version()}, these bindings mirror version "
+                               f"{ABI_VERSION}: rebuild it with __graft_entry__.build()")
         _lib = L
     return _lib
 

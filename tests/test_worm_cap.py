@@ -3,16 +3,25 @@
 With S=1 Heisenberg tables the first thermalisation sweeps, while the cutoff L is still
 small, can run worms that are orders of magnitude longer than the opstring.  They close
 in the end, but the tail is heavy (over 10^9 steps in some chains).  The reference's
-worm_traverse! (src/sse.jl:262-303) has no length limit and runs such a worm to its end;
-the oracle and the engine stop the walker after 64 * (L + 16) steps with status 8 (worm
-cap).  This file pins one such walker on the CPU, checks that the same worm closes under
-a larger cap, and on the GPU checks that the engine stops it identically while the other
-walkers of its batch finish normally."""
+worm_traverse! (src/sse.jl:262-303) has no length limit and runs such a worm to its end.
+The oracle and the engine cap a worm at 64 * (L + 16) steps:
+
+* during thermalisation the sweep's worm phase is undone: the opstring returns to its state
+  after the diagonal update, the worm-count controller and the spin state stay as they were,
+  and the walker goes on (thermalisation sweeps need no detailed balance);
+* after thermalisation the walker stops with status 8 (worm cap).
+
+This file pins one such walker on the CPU in both phases, checks that the same worm closes
+under a larger cap and that chains thermalised with many undone sweeps still sample the ED
+values, and on the GPU checks that the engine does exactly what the oracle does."""
 
 import numpy as np
 import pytest
 
-LONG_WORM = dict(S=1.0, lattice="bilayer", side=6, beta=8.0, seed=99, stream=7, thermalization=100, sweep=1)
+# the walker's second sweep (sweeps == 1) runs a worm of 145,785 steps > 64 * (2171 + 16)
+LONG_WORM = dict(S=1.0, lattice="bilayer", side=6, beta=8.0, seed=99, stream=7, sweep=1)
+MEASURED = 0  # thermalization: the long worm falls in a measured sweep and stops the walker
+THERMALISING = 100  # thermalization: the long worm's sweep is undone
 
 
 def long_worm_model(S):
@@ -21,15 +30,114 @@ def long_worm_model(S):
     return S.flatten_model(S.MagnetModel(model_params(LONG_WORM["S"], LONG_WORM["lattice"], LONG_WORM["side"])))
 
 
-def test_oracle_stops_long_worm_at_cap(S, O):
+def oracle_walker(O, om, thermalization, factor=None):
+    w = O.OracleWalker(om, T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=LONG_WORM["stream"],
+                       thermalization=thermalization)
+    if factor is not None:
+        w.w.worm_cap_factor = factor
+    w.init()
+    return w
+
+
+def test_oracle_stops_long_worm_in_measured_sweep(S, O):
+    om = O.OracleModel(long_worm_model(S))
+    w = oracle_walker(O, om, MEASURED)
+    with pytest.raises(RuntimeError):
+        w.run(10, measure=False)
+    assert w.w.status == 8 and w.w.sweeps == LONG_WORM["sweep"] and w.w.worm_undos == 0
+
+
+def test_oracle_undoes_long_worm_in_thermalisation(S, O):
+    """The sweep's worm phase is undone: the opstring is again the diagonal update's, and the spin
+    state, operator count and worm-count controller are those before the worm phase; the draws
+    the worm consumed stay consumed."""
+    from test_oracle import isconsistent
+
     flat = long_worm_model(S)
     om = O.OracleModel(flat)
-    w = O.OracleWalker(om, T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=LONG_WORM["stream"], thermalization=LONG_WORM["thermalization"])
-    w.init()
-    with pytest.raises(RuntimeError):
-        for _ in range(10):
-            w.step(measure=False)
-    assert w.w.status == 8 and w.w.sweeps == LONG_WORM["sweep"]
+    w = oracle_walker(O, om, THERMALISING)
+    w.run(LONG_WORM["sweep"], measure=False)
+    w.diagonal_update(thermalized=False)
+    w.make_vertex_list()
+    ops, st, before = w.ops, w.state, w.scalars()
+    w.worm_update(thermalized=False)
+    after = w.scalars()
+    assert w.w.worm_undos == 1 and after["status"] == 0
+    assert np.array_equal(w.ops, ops) and np.array_equal(w.state, st) and isconsistent(flat, w.ops, w.state)
+    for k in ("L", "n", "num_worms", "avg_worm_length"):
+        assert after[k] == before[k], k
+    assert after["ctr"] > before["ctr"] + 64 * (2171 + 16)
+    # the same walker through whole Carlo steps: one undone sweep, then it sweeps on
+    w = oracle_walker(O, om, THERMALISING)
+    w.run(5, measure=False)
+    assert w.w.status == 0 and w.w.sweeps == 5 and w.w.worm_undos == 1
+    assert isconsistent(flat, w.ops, w.state)
+
+
+def test_oracle_stopped_worm_closes_under_larger_cap(S, O):
+    """The stopped worm is long, not endless: at 64 * (L + 16) = 139,968 steps it is cut off, and
+    with a cap of 1000 * (L + 16) the same trajectory closes it and sweeps on."""
+    flat = long_worm_model(S)
+    w = oracle_walker(O, O.OracleModel(flat), MEASURED, factor=1000)
+    w.run(3, measure=False)
+    assert w.w.status == 0 and w.w.sweeps == 3 and w.w.worm_undos == 0
+    assert w.w.worm_steps_total > 64 * (2171 + 16)
+
+
+def test_oracle_smaller_cap_stops_sooner(S, O):
+    """A smaller cap factor ends the same long worm after fewer steps."""
+    om = O.OracleModel(long_worm_model(S))
+    steps = {}
+    for factor in (64, 4):
+        w = oracle_walker(O, om, MEASURED, factor=factor)
+        with pytest.raises(RuntimeError):
+            w.run(5, measure=False)
+        assert w.w.status == 8 and w.w.sweeps == LONG_WORM["sweep"]
+        steps[factor] = w.w.worm_steps_total
+    assert steps[4] < steps[64]
+
+
+def test_oracle_chains_with_undone_sweeps_sample_ed(S, O):
+    """Chains thermalised under a cap of 1 * (L + 16), which undoes about one thermalisation sweep
+    in fifty, then measured under the default cap, still give the exact-diagonalisation values
+    (mixed S=1/2 / S=1 honeycomb job at T = 0.7, |z| <= 4 as in the ED comparison)."""
+    from ed import ed_observables, evaluables, jackknife
+    from test_ed_compare import JOBS, make_model, obs_names
+
+    T, therm, nbins, binsize = 0.7, 1000, 16, 400
+    model = make_model(S, JOBS["honeycomb"])
+    flat = S.flatten_model(model)
+    om = O.OracleModel(flat)
+    names = obs_names(flat.est_prefixes)
+    bins = {n: [] for n in names}
+    walkers = []
+    for k in range(4):
+        w = O.OracleWalker(om, T=T, seed=124535, stream=k, thermalization=therm)
+        w.w.worm_cap_factor = 1
+        w.init()
+        w.run(therm, measure=True)
+        w.w.worm_cap_factor = 64
+        walkers.append(w)
+    assert all(w.w.worm_undos >= 5 for w in walkers)
+    prev = [w.obs()[:2] for w in walkers]
+    for _ in range(nbins):
+        for k, w in enumerate(walkers):
+            w.run(binsize, measure=True)
+            s, c, _ = w.obs()
+            ds, dc = s - prev[k][0], c - prev[k][1]
+            prev[k] = (s, c)
+            for i, n in enumerate(names):
+                bins[n].append(ds[i] / max(dc[i], 1))
+    bins = {n: np.array(v) for n, v in bins.items()}
+    ed = ed_observables(S, model, [T])
+    bad = []
+    for name, f in evaluables(flat.est_prefixes, flat.norm_site_count).items():
+        mc, err = jackknife(bins, f)
+        z = abs(mc - float(ed[name][0])) / (err if err != 0 else 1e-8)
+        if z > 4:
+            bad.append((name, mc, err, float(ed[name][0]), z))
+    assert not bad, bad
+    assert all(w.w.status == 0 for w in walkers)
 
 
 @pytest.mark.gpu
@@ -39,7 +147,7 @@ def test_engine_stops_long_worm_walker_like_oracle(S, O):
     flat = long_worm_model(S)
     eng = Engine(0)
     mid = eng.register_model(flat)
-    params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=LONG_WORM["thermalization"])
+    params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=MEASURED)
               for s in (LONG_WORM["stream"], 0, 1, 2)]
     ids = eng.create_walkers(mid, params)
     eng.init(ids)
@@ -47,11 +155,9 @@ def test_engine_stops_long_worm_walker_like_oracle(S, O):
         eng.sweep(ids, 5, measure=False)
     assert err.value.code == 8
     inf = eng.info(int(ids[0]))
-    assert inf["status"] == 8 and inf["sweeps"] == LONG_WORM["sweep"]
+    assert inf["status"] == 8 and inf["sweeps"] == LONG_WORM["sweep"] and inf["worm_undos"] == 0
     # the stopped walker's opstring and counters match the oracle at the cap
-    om = O.OracleModel(flat)
-    w = O.OracleWalker(om, T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=LONG_WORM["stream"], thermalization=LONG_WORM["thermalization"])
-    w.init()
+    w = oracle_walker(O, O.OracleModel(flat), MEASURED)
     with pytest.raises(RuntimeError):
         w.run(5, measure=False)
     ops, st, inf = eng.export(int(ids[0]))
@@ -65,36 +171,30 @@ def test_engine_stops_long_worm_walker_like_oracle(S, O):
     eng.close()
 
 
-def test_oracle_stopped_worm_closes_under_larger_cap(S, O):
-    """The stopped worm is long, not endless: at 64 * (L + 16) = 139,968 steps it is cut off, and
-    with a cap of 1000 * (L + 16) the same trajectory closes it and sweeps on."""
+@pytest.mark.gpu
+@pytest.mark.parametrize("staging", [0, 48 * 1024])
+def test_engine_undoes_long_worm_like_oracle(S, O, staging):
+    """During thermalisation the engine undoes the long worm's sweep exactly as the oracle does
+    (records chased in HBM, and staged in shared memory), and the walker sweeps on bit for bit."""
     flat = long_worm_model(S)
-    om = O.OracleModel(flat)
-    w = O.OracleWalker(om, T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=LONG_WORM["stream"],
-                       thermalization=LONG_WORM["thermalization"])
-    w.w.worm_cap_factor = 1000
-    w.init()
-    w.run(3, measure=False)
-    assert w.w.status == 0 and w.w.sweeps == 3
-    assert w.w.worm_steps_total > 64 * (2171 + 16)
-    assert w.state.shape == (flat.nsites,)
+    from sse_gb300.engine import Engine
 
-
-def test_oracle_smaller_cap_stops_sooner(S, O):
-    """A smaller cap factor ends the same long worm after fewer steps."""
-    flat = long_worm_model(S)
-    om = O.OracleModel(flat)
-    steps = {}
-    for factor in (64, 4):
-        w = O.OracleWalker(om, T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=LONG_WORM["stream"],
-                           thermalization=LONG_WORM["thermalization"])
-        w.w.worm_cap_factor = factor
-        w.init()
-        with pytest.raises(RuntimeError):
-            w.run(5, measure=False)
-        assert w.w.status == 8 and w.w.sweeps == LONG_WORM["sweep"]
-        steps[factor] = w.w.worm_steps_total
-    assert steps[4] < steps[64]
+    eng = Engine(0)
+    eng.set_staging(staging)
+    mid = eng.register_model(flat)
+    ids = eng.create_walkers(mid, [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s,
+                                        thermalization=THERMALISING) for s in (LONG_WORM["stream"], 0)])
+    eng.init(ids)
+    eng.sweep(ids, 5, measure=False)
+    w = oracle_walker(O, O.OracleModel(flat), THERMALISING)
+    w.run(5, measure=False)
+    ops, st, inf = eng.export(int(ids[0]))
+    assert inf["status"] == 0 and inf["sweeps"] == 5 and inf["worm_undos"] == w.w.worm_undos == 1
+    assert inf["rng_counter"] == w.w.ctr and inf["worm_steps"] == w.w.worm_steps_total
+    assert inf["num_worms"] == w.w.num_worms and inf["avg_worm_length"] == w.w.avg_worm_length
+    assert np.array_equal(ops, w.ops) and np.array_equal(st, w.state)
+    assert eng.check(ids).tolist() == [0, 0]
+    eng.close()
 
 
 @pytest.mark.gpu
@@ -105,16 +205,12 @@ def test_engine_worm_cap_factor_matches_oracle(S, O):
     eng = Engine(0)
     mid = eng.register_model(flat)
     ids = eng.create_walkers(mid, [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=LONG_WORM["stream"],
-                                        thermalization=LONG_WORM["thermalization"])])
+                                        thermalization=MEASURED)])
     eng.set_worm_cap(ids, 4)
     eng.init(ids)
     with pytest.raises(SSEError):
         eng.sweep(ids, 5, measure=False)
-    om = O.OracleModel(flat)
-    w = O.OracleWalker(om, T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=LONG_WORM["stream"],
-                       thermalization=LONG_WORM["thermalization"])
-    w.w.worm_cap_factor = 4
-    w.init()
+    w = oracle_walker(O, O.OracleModel(flat), MEASURED, factor=4)
     with pytest.raises(RuntimeError):
         w.run(5, measure=False)
     ops, st, inf = eng.export(int(ids[0]))
