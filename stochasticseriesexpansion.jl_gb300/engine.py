@@ -13,6 +13,9 @@ import numpy as np
 
 from .build import LIB
 
+# SSE_GPU_ABI_VERSION of include/sse_gpu.h whose structs these bindings mirror
+ABI_VERSION = 2
+
 P = C.POINTER
 
 SSE_SWEEP_MEASURE = 1
@@ -141,6 +144,9 @@ def lib():
             f = getattr(L, name)
             f.argtypes = args
             f.restype = res
+        if L.sse_abi_version() != ABI_VERSION:
+            raise RuntimeError(f"{LIB} has ABI version {L.sse_abi_version()}, these bindings mirror version "
+                               f"{ABI_VERSION}: rebuild it with __graft_entry__.build()")
         _lib = L
     return _lib
 

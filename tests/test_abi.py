@@ -41,3 +41,53 @@ def test_binding_covers_header():
     from sse_gb300.engine import exported_symbols
 
     assert set(exported_symbols()) >= set(declared_symbols())
+
+
+def test_abi_version_matches_header_and_bindings():
+    """The structs of engine.py mirror the header's; the library reports the same version (a plain
+    C function: nothing touches the GPU)."""
+    from sse_gb300 import build as B
+    from sse_gb300.engine import ABI_VERSION
+
+    src = open(os.path.join(ROOT, "include", "sse_gpu.h")).read()
+    (hv,) = re.findall(r"#define SSE_GPU_ABI_VERSION (\d+)", src)
+    assert int(hv) == ABI_VERSION
+    try:
+        path = B.build()
+    except (FileNotFoundError, OSError) as e:  # no nvcc on this machine
+        pytest.skip(f"nvcc unavailable: {e}")
+    lib = ctypes.CDLL(path)
+    lib.sse_abi_version.restype = ctypes.c_int
+    assert lib.sse_abi_version() == ABI_VERSION
+
+
+def test_ctypes_structs_match_header_layout(tmp_path):
+    """Every field offset and the size of the four ABI structs, as the C compiler lays them out
+    from include/sse_gpu.h, equal those of the ctypes mirrors in engine.py."""
+    import shutil
+    import subprocess
+
+    from sse_gb300.engine import ModelDesc, NoAllocWalker, WalkerInfo, WalkerParams
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"sse_model_desc": ModelDesc, "sse_walker_params": WalkerParams, "sse_walker_info": WalkerInfo,
+               "sse_noalloc_walker": NoAllocWalker}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "sse_gpu.h"', "int main(void) {"]
+    for cname, cls in mirrors.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for field, _ in cls._fields_:
+            lines.append(f'  printf("{cname} {field} %zu\\n", offsetof({cname}, {field}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {(a, b): int(c) for a, b, c in (ln.split() for ln in out if ln)}
+    for cname, cls in mirrors.items():
+        assert got[(cname, "size")] == ctypes.sizeof(cls), cname
+        for field, _ in cls._fields_:
+            assert got[(cname, field)] == getattr(cls, field).offset, (cname, field)
+
