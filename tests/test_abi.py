@@ -123,12 +123,16 @@ def test_model_table_conversion():
 
 
 def test_flattened_tables_need_no_conversion(S):
-    """The host builder already emits every table in its C type, so registration copies nothing."""
+    """The host builder already emits every table of every model family in its C type, so
+    registration passes the builder's own arrays."""
     import numpy as np
 
     from sse_gb300.engine import MODEL_TABLES, model_table
+    from test_tables import families
 
-    flat = S.flatten_model(S.MagnetModel({"lattice": {"unitcell": S.UnitCells.square, "size": (4, 4)}, "J": 1.0}))
-    for name, dt in MODEL_TABLES:
-        assert flat.arrays[name].dtype == dt, name
-        assert np.shares_memory(model_table(flat.arrays, name, dt), flat.arrays[name]) or flat.arrays[name].size == 0
+    for family, make in families(S).items():
+        flat = S.flatten_model(make(S))
+        for name, dt in MODEL_TABLES:
+            arr = flat.arrays[name]
+            assert arr.dtype == dt and arr.flags.c_contiguous, (family, name)
+            assert arr.size == 0 or np.shares_memory(model_table(flat.arrays, name, dt), arr), (family, name)
