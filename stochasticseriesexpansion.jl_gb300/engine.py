@@ -192,6 +192,27 @@ def _p(a, t):
     return a.ctypes.data_as(P(t))
 
 
+# the flat model tables in sse_model_desc order, with their C element types
+MODEL_TABLES = (
+    ("site_dims", np.int32), ("bond_type", np.int32), ("bond_sites", np.int32), ("type_dims", np.int32),
+    ("type_nverts", np.int32), ("type_maxworm", np.int32), ("type_diag_off", np.int32), ("type_vert_off", np.int32),
+    ("type_trans_off", np.int32), ("diag_vertex", np.int32), ("weight", np.float64), ("sign", np.int8),
+    ("leg_state", np.uint8), ("trans_start", np.int32), ("trans_count", np.int32), ("out_cum", np.float64),
+    ("out_target", np.int32), ("out_leg", np.int8), ("out_worm", np.int8), ("est_coef", np.float64),
+)
+_CTYPE = {np.int32: C.c_int32, np.float64: C.c_double, np.int8: C.c_int8, np.uint8: C.c_uint8}
+
+
+def model_table(arrays, name, dtype):
+    """arrays[name] as a C-contiguous array of the table's C element type; a conversion that would
+    change a value (overflow, a fraction in an integer table) raises ValueError."""
+    x = np.asarray(arrays[name])
+    y = np.ascontiguousarray(x.reshape(-1), dtype=dtype)
+    if x.dtype != y.dtype and not np.array_equal(y, x.reshape(-1)):
+        raise ValueError(f"model table {name!r}: values do not fit {np.dtype(dtype).name}")
+    return y
+
+
 def _ids(ids):
     a = np.ascontiguousarray(ids, dtype=np.int32)
     return a, _p(a, C.c_int32)
@@ -226,21 +247,15 @@ class Engine:
 
     # ---- models ----
     def register_model(self, flat) -> int:
-        a = flat.arrays
-        keep = dict(a)
+        # converted copies stay referenced here until the library has copied them to the device
+        tables = [model_table(flat.arrays, name, dt) for name, dt in MODEL_TABLES]
         d = ModelDesc(
             flat.nsites, flat.nbonds, flat.ntypes, flat.maxdim, flat.nest, flat.energy_offset, flat.norm_site_count,
-            _p(a["site_dims"], C.c_int32), _p(a["bond_type"], C.c_int32), _p(a["bond_sites"], C.c_int32),
-            _p(a["type_dims"], C.c_int32), _p(a["type_nverts"], C.c_int32), _p(a["type_maxworm"], C.c_int32),
-            _p(a["type_diag_off"], C.c_int32), _p(a["type_vert_off"], C.c_int32), _p(a["type_trans_off"], C.c_int32),
-            _p(a["diag_vertex"], C.c_int32), _p(a["weight"], C.c_double), _p(a["sign"], C.c_int8),
-            _p(a["leg_state"], C.c_uint8), _p(a["trans_start"], C.c_int32), _p(a["trans_count"], C.c_int32),
-            _p(a["out_cum"], C.c_double), _p(a["out_target"], C.c_int32), _p(a["out_leg"], C.c_int8),
-            _p(a["out_worm"], C.c_int8), _p(a["est_coef"], C.c_double),
+            *[_p(t, _CTYPE[dt]) for t, (_, dt) in zip(tables, MODEL_TABLES)],
         )
         mid = C.c_int32()
         self._check(self._L.sse_model_register(self.h, C.byref(d), C.byref(mid)))
-        del keep
+        del tables
         self._models[mid.value] = flat
         return mid.value
 

@@ -204,20 +204,32 @@ class BatchMC:
 
 
 def jackknife_results(bins: list, names: list, flat) -> dict:
-    """Evaluables with jackknife errors over bins (dicts of observable means): name -> (mean, error)."""
+    """Evaluables with jackknife errors over bins (dicts of observable means): name -> (mean, error).
+
+    A bin without measurements (NaN means: a walker that measured nothing in it) is left out, so it
+    does not pull the means towards zero; with fewer than two bins the errors are NaN."""
     keys = [k for k in names if not all(np.isnan(b[k]) for b in bins)]
-    arr = {k: np.array([b[k] for b in bins]) for k in keys}
+    bins = [b for b in bins if not any(np.isnan(b[k]) for k in keys)]
     nb = len(bins)
-    tot = {k: np.nansum(v) for k, v in arr.items()}
+    if nb == 0 or not keys:
+        return {}
+    arr = {k: np.array([b[k] for b in bins]) for k in keys}
+    tot = {k: v.sum() for k, v in arr.items()}
     full = evaluables({k: tot[k] / nb for k in keys}, flat.est_prefixes, flat.norm_site_count)
+    res = {}
+    if nb < 2:
+        for name, v in full.items():
+            res[name] = (v, float("nan"))
+        for k in keys:
+            res.setdefault(k, (float(arr[k][0]), float("nan")))
+        return res
     loo = [evaluables({k: (tot[k] - arr[k][i]) / (nb - 1) for k in keys}, flat.est_prefixes, flat.norm_site_count)
            for i in range(nb)]
-    res = {}
     for name, v in full.items():
         x = np.array([l[name] for l in loo])
         res[name] = (v, float(np.sqrt((nb - 1) / nb * np.sum((x - x.mean()) ** 2))))
     for k in keys:
-        res.setdefault(k, (float(np.nanmean(arr[k])), float(np.nanstd(arr[k]) / np.sqrt(max(nb, 1)))))
+        res.setdefault(k, (float(arr[k].mean()), float(arr[k].std() / np.sqrt(nb))))
     return res
 
 

@@ -91,3 +91,48 @@ def test_ctypes_structs_match_header_layout(tmp_path):
         for field, _ in cls._fields_:
             assert got[(cname, field)] == getattr(cls, field).offset, (cname, field)
 
+
+
+def test_model_tables_follow_desc_order_and_types():
+    """register_model fills sse_model_desc's pointers from MODEL_TABLES in order, with the element
+    type each pointer field declares."""
+    from sse_gb300.engine import _CTYPE, MODEL_TABLES, ModelDesc
+
+    ptr_fields = [(f, t) for f, t in ModelDesc._fields_ if issubclass(t, ctypes._Pointer)]
+    assert [f for f, _ in ptr_fields] == [n for n, _ in MODEL_TABLES]
+    for (f, t), (_, dt) in zip(ptr_fields, MODEL_TABLES):
+        assert t._type_ is _CTYPE[dt], f
+
+
+def test_model_table_conversion():
+    import numpy as np
+
+    from sse_gb300.engine import model_table
+
+    # a wider integer type and a strided view are converted to contiguous int32
+    a = {"bond_sites": np.arange(12, dtype=np.int64)[::2]}
+    t = model_table(a, "bond_sites", np.int32)
+    assert t.dtype == np.int32 and t.flags.c_contiguous and t.tolist() == list(range(0, 12, 2))
+    # a conversion that changes values is refused
+    with pytest.raises(ValueError):
+        model_table({"bond_type": np.array([1 << 40])}, "bond_type", np.int32)
+    with pytest.raises(ValueError):
+        model_table({"leg_state": np.array([0.5])}, "leg_state", np.uint8)
+    with pytest.raises(ValueError):
+        model_table({"leg_state": np.array([-1])}, "leg_state", np.uint8)
+
+
+def test_flattened_tables_need_no_conversion(S):
+    """The host builder already emits every table of every model family in its C type, so
+    registration passes the builder's own arrays."""
+    import numpy as np
+
+    from sse_gb300.engine import MODEL_TABLES, model_table
+    from test_tables import families
+
+    for family, make in families(S).items():
+        flat = S.flatten_model(make(S))
+        for name, dt in MODEL_TABLES:
+            arr = flat.arrays[name]
+            assert arr.dtype == dt and arr.flags.c_contiguous, (family, name)
+            assert arr.size == 0 or np.shares_memory(model_table(flat.arrays, name, dt), arr), (family, name)

@@ -146,3 +146,23 @@ def test_tempering_mc_bins_follow_the_temperature(S):
     assert pt.acceptance()[0] == 1.0 and np.isnan(pt.acceptance()[1])
     with pytest.raises(ValueError):
         TemperingMC(p, [0.5, 0.5], engine=eng)
+
+
+def test_jackknife_skips_empty_bins_and_single_bin(S):
+    """A bin in which a walker measured nothing (NaN means) is left out instead of counting as zero;
+    one bin gives means with NaN errors instead of a division by zero."""
+    from sse_gb300.mc import jackknife_results, observable_names
+
+    flat = S.flatten_model(S.MagnetModel({"lattice": {"unitcell": S.UnitCells.square, "size": (2, 2)}, "J": 1.0,
+                                          "measure": ["magnetization"]}))
+    names = observable_names(flat.est_prefixes)
+    rng = np.random.default_rng(4)
+    full = [{n: float(v) for n, v in zip(names, rng.uniform(0.5, 1.5, len(names)))} for _ in range(6)]
+    empty = {n: float("nan") for n in names}
+    with_empty = jackknife_results(full[:3] + [empty] + full[3:], names, flat)
+    without = jackknife_results(full, names, flat)
+    for k, (m, e) in without.items():
+        assert with_empty[k][0] == pytest.approx(m, rel=1e-12) and with_empty[k][1] == pytest.approx(e, rel=1e-12)
+    one = jackknife_results(full[:1], names, flat)
+    assert one["Energy"][0] == pytest.approx(full[0]["SignEnergy"] / full[0]["Sign"]) and math.isnan(one["Energy"][1])
+    assert jackknife_results([empty], names, flat) == {}
