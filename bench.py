@@ -348,7 +348,9 @@ def run_other_workload(args):
              "parameter_map": {"J": ["Jp", "J", "J", "J", "J"]}, "Dz": 0.3, "hz": 0.2, "measure": ["magnetization"]}
         mid = eng.register_model(S.flatten_model(S.MagnetModel(p)))
         betas = [4.0, 8.0, 16.0]
-        params = [(mid, dict(T=1.0 / betas[k % 3], seed=args.seed, stream=k, thermalization=10**9))
+        # the walkers count the first --therm sweeps as thermalisation (Carlo's rule), so the timed
+        # steps run measure! and the worm-count controller is frozen, as in a production run
+        params = [(mid, dict(T=1.0 / betas[k % 3], seed=args.seed, stream=k, thermalization=args.therm))
                   for k in range(2048)]
         desc = "2048 walkers, S=1 square bilayer 48x48, J=1, J_perp=0.5, Dz=0.3, hz=0.2, beta in {4,8,16}"
         ids = []
