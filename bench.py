@@ -308,7 +308,8 @@ def run_other_workload(args):
 
         flat = S.flatten_model(make_model(S, 8))
         mid = eng.register_model(flat)
-        a, b = eng.create_walkers(mid, [dict(T=0.5, seed=args.seed, stream=0, thermalization=10**4)] * 2)
+        # 2000 thermalisation sweeps, then every timed sweep runs measure! (GPU and CPU alike)
+        a, b = eng.create_walkers(mid, [dict(T=0.5, seed=args.seed, stream=0, thermalization=2000)] * 2)
         eng.init([a, b])
         eng.sweep([a, b], 2000, measure=False)
         n = 20000
@@ -330,7 +331,7 @@ def run_other_workload(args):
         eng.sweep([b], 500, measure=True, graph=True)
         graph_ms, _ = eng.last_timing()
         om = O.OracleModel(flat)
-        w = O.OracleWalker(om, T=0.5, seed=args.seed, stream=0, thermalization=10**4)
+        w = O.OracleWalker(om, T=0.5, seed=args.seed, stream=0, thermalization=2000)
         w.init()
         w.run(2000, measure=False)
         t0 = time.perf_counter()
