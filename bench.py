@@ -308,7 +308,8 @@ def run_other_workload(args):
 
         flat = S.flatten_model(make_model(S, 8))
         mid = eng.register_model(flat)
-        a, b = eng.create_walkers(mid, [dict(T=0.5, seed=args.seed, stream=0, thermalization=10**4)] * 2)
+        # 2000 thermalisation sweeps, then every timed sweep runs measure! (GPU and CPU alike)
+        a, b = eng.create_walkers(mid, [dict(T=0.5, seed=args.seed, stream=0, thermalization=2000)] * 2)
         eng.init([a, b])
         eng.sweep([a, b], 2000, measure=False)
         n = 20000
@@ -330,7 +331,7 @@ def run_other_workload(args):
         eng.sweep([b], 500, measure=True, graph=True)
         graph_ms, _ = eng.last_timing()
         om = O.OracleModel(flat)
-        w = O.OracleWalker(om, T=0.5, seed=args.seed, stream=0, thermalization=10**4)
+        w = O.OracleWalker(om, T=0.5, seed=args.seed, stream=0, thermalization=2000)
         w.init()
         w.run(2000, measure=False)
         t0 = time.perf_counter()
@@ -348,7 +349,9 @@ def run_other_workload(args):
              "parameter_map": {"J": ["Jp", "J", "J", "J", "J"]}, "Dz": 0.3, "hz": 0.2, "measure": ["magnetization"]}
         mid = eng.register_model(S.flatten_model(S.MagnetModel(p)))
         betas = [4.0, 8.0, 16.0]
-        params = [(mid, dict(T=1.0 / betas[k % 3], seed=args.seed, stream=k, thermalization=10**9))
+        # the walkers count the first --therm sweeps as thermalisation (Carlo's rule), so the timed
+        # steps run measure! and the worm-count controller is frozen, as in a production run
+        params = [(mid, dict(T=1.0 / betas[k % 3], seed=args.seed, stream=k, thermalization=args.therm))
                   for k in range(2048)]
         desc = "2048 walkers, S=1 square bilayer 48x48, J=1, J_perp=0.5, Dz=0.3, hz=0.2, beta in {4,8,16}"
         ids = []

@@ -560,6 +560,17 @@ int upload(sse_engine *e, HostModel &hm, const T *src, size_t count, const T **d
   return SSE_OK;
 }
 
+void free_walker_buffers(sse_engine *e, HostWalker &h) {
+  dev_free(e, h.ops);
+  dev_free(e, h.rec);
+  dev_free(e, h.cidx);
+  dev_free(e, h.vfirst);
+  dev_free(e, h.state);
+  dev_free(e, h.obs_sum);
+  dev_free(e, h.obs_last);
+  dev_free(e, h.obs_count);
+}
+
 bool valid_id(sse_engine *e, int32_t id) {
   return id >= 0 && (size_t)id < e->walkers.size() && e->walkers[id].alive;
 }
@@ -578,13 +589,25 @@ int check_work_ids(sse_engine *e, int32_t count, const int32_t *ids) {
 int ensure_work(sse_engine *e, size_t n) {
   if (n <= e->work_cap) return SSE_OK;
   size_t cap = std::max<size_t>(n, 2 * e->work_cap);
+  // allocate the new buffers before freeing the old ones: a failure leaves the engine as it was
+  decltype(e->d_work) work = nullptr;
+  decltype(e->d_status) status = nullptr;
+  decltype(e->d_needL) needL = nullptr;
+  int rc = dev_alloc(e, &work, cap);
+  if (!rc) rc = dev_alloc(e, &status, cap);
+  if (!rc) rc = dev_alloc(e, &needL, cap);
+  if (rc) {
+    dev_free(e, work);
+    dev_free(e, status);
+    dev_free(e, needL);
+    return rc;
+  }
   dev_free(e, e->d_work);
   dev_free(e, e->d_status);
   dev_free(e, e->d_needL);
-  int rc = dev_alloc(e, &e->d_work, cap);
-  if (!rc) rc = dev_alloc(e, &e->d_status, cap);
-  if (!rc) rc = dev_alloc(e, &e->d_needL, cap);
-  if (rc) return rc;
+  e->d_work = work;
+  e->d_status = status;
+  e->d_needL = needL;
   e->work_cap = cap;
   e->status_cap = cap;
   return SSE_OK;
@@ -618,9 +641,22 @@ int grow_walker(sse_engine *e, int32_t id, long long need) {
   rc = dev_alloc(e, &ops, (size_t)cap);
   if (!rc) rc = dev_alloc(e, &rec, (size_t)cap);
   if (!rc) rc = dev_alloc(e, &cidx, (size_t)cap);
-  if (rc) return rc;
-  if (h.ops && w.L > 0)
-    CUDA_TRY(e, cudaMemcpyAsync(ops, h.ops, sizeof(uint32_t) * (size_t)w.L, cudaMemcpyDeviceToDevice, e->stream));
+  if (rc) {
+    dev_free(e, ops);
+    dev_free(e, rec);
+    dev_free(e, cidx);
+    return rc;
+  }
+  if (h.ops && w.L > 0) {
+    const cudaError_t st =
+        cudaMemcpyAsync(ops, h.ops, sizeof(uint32_t) * (size_t)w.L, cudaMemcpyDeviceToDevice, e->stream);
+    if (st != cudaSuccess) {
+      dev_free(e, ops);
+      dev_free(e, rec);
+      dev_free(e, cidx);
+      return fail(e, SSE_ERR_CUDA, std::string("cudaMemcpyAsync (opstring prefix): ") + cudaGetErrorString(st));
+    }
+  }
   dev_free(e, h.ops);
   dev_free(e, h.rec);
   dev_free(e, h.cidx);
@@ -841,11 +877,14 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
 
 int upload_models(sse_engine *e) {
   if (e->models.size() > e->d_models_cap) {
+    // allocate the new array before freeing the old one: a failure leaves the engine as it was
+    size_t cap = std::max<size_t>(8, 2 * e->models.size());
+    DevModel *nm = nullptr;
+    int rc = dev_alloc(e, &nm, cap);
+    if (rc) return rc;
     clear_graphs(e);
     dev_free(e, e->d_models);
-    size_t cap = std::max<size_t>(8, 2 * e->models.size());
-    int rc = dev_alloc(e, &e->d_models, cap);
-    if (rc) return rc;
+    e->d_models = nm;
     e->d_models_cap = cap;
   }
   std::vector<DevModel> h(e->models.size());
@@ -920,16 +959,7 @@ int sse_engine_destroy(sse_engine *e) {
   if (!e) return SSE_ERR_ARG;
   cudaSetDevice(e->device);
   clear_graphs(e);
-  for (auto &w : e->walkers) {
-    dev_free(e, w.ops);
-    dev_free(e, w.rec);
-    dev_free(e, w.cidx);
-    dev_free(e, w.vfirst);
-    dev_free(e, w.state);
-    dev_free(e, w.obs_sum);
-    dev_free(e, w.obs_last);
-    dev_free(e, w.obs_count);
-  }
+  for (auto &w : e->walkers) free_walker_buffers(e, w);
   for (auto &m : e->models)
     for (void *p : m.allocs) cudaFreeAsync(p, e->stream);
   dev_free(e, e->d_models);
@@ -957,6 +987,16 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
   if (d->maxdim < 2 || d->maxdim > 255) return fail(e, SSE_ERR_UNSUPPORTED, "site dimension must be 2..255");
   cudaSetDevice(e->device);
   HostModel hm;
+  // every table uploaded below is freed again when the registration fails, on any path
+  struct Uploads {
+    sse_engine *e;
+    HostModel &hm;
+    bool keep;
+    ~Uploads() {
+      if (!keep)
+        for (void *p : hm.allocs) cudaFreeAsync(p, e->stream);
+    }
+  } uploads{e, hm, false};
   hm.nsites = d->nsites;
   hm.nobs = 6 + 5 * d->nest;
   DevModel &m = hm.dev;
@@ -1120,13 +1160,14 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
     if (!ok) c2.assign(1, 0);
     if (!rc) rc = upload(e, hm, c2.data(), c2.size(), &m.est_coef2);
   }
-  if (rc) {
-    for (void *p : hm.allocs) cudaFreeAsync(p, e->stream);
-    return rc;
-  }
+  if (rc) return rc;
   e->models.push_back(hm);
   rc = upload_models(e);
-  if (rc) return rc;
+  if (rc) {
+    e->models.pop_back();
+    return rc;
+  }
+  uploads.keep = true;
   *model_id = (int32_t)e->models.size() - 1;
   return SSE_OK;
 }
@@ -1142,15 +1183,30 @@ int sse_walkers_create(sse_engine *e, int32_t model_id, int32_t count, const sse
   if (!e || !params || !ids || count < 0 || model_id < 0 || (size_t)model_id >= e->models.size())
     return SSE_ERR_ARG;
   cudaSetDevice(e->device);
-  const HostModel &hm = e->models[model_id];
-  const size_t first = e->walkers.size();
-  int rc = ensure_walker_slots(e, first + count);
-  if (rc) return rc;
-  std::vector<DevWalker> dw(count);
+  // all parameters are checked before anything is allocated
   for (int i = 0; i < count; i++) {
     const sse_walker_params &p = params[i];
     if (!(p.T > 0) || p.diagonal_warmup_sweeps < 0 || !(p.init_num_worms >= 0))
       return fail(e, SSE_ERR_ARG, "walker parameters out of range");
+  }
+  const HostModel &hm = e->models[model_id];
+  const size_t first = e->walkers.size();
+  int rc = ensure_walker_slots(e, first + count);
+  if (rc) return rc;
+  // on a failure below, the walkers of this call are freed again and their ids never handed out
+  struct Created {
+    sse_engine *e;
+    size_t first;
+    bool keep;
+    ~Created() {
+      if (keep) return;
+      for (size_t k = first; k < e->walkers.size(); k++) free_walker_buffers(e, e->walkers[k]);
+      e->walkers.resize(first);
+    }
+  } created{e, first, false};
+  std::vector<DevWalker> dw(count);
+  for (int i = 0; i < count; i++) {
+    const sse_walker_params &p = params[i];
     HostWalker h;
     h.alive = true;
     h.model = model_id;
@@ -1165,6 +1221,7 @@ int sse_walkers_create(sse_engine *e, int32_t model_id, int32_t count, const sse
     if (!rc) rc = dev_alloc(e, &h.obs_sum, (size_t)hm.nobs);
     if (!rc) rc = dev_alloc(e, &h.obs_last, (size_t)hm.nobs);
     if (!rc) rc = dev_alloc(e, &h.obs_count, (size_t)hm.nobs);
+    e->walkers.push_back(h);  // from here on the guard frees its buffers if the call fails
     if (rc) return rc;
     CUDA_TRY(e, cudaMemsetAsync(h.obs_sum, 0, sizeof(double) * hm.nobs, e->stream));
     CUDA_TRY(e, cudaMemsetAsync(h.obs_last, 0, sizeof(double) * hm.nobs, e->stream));
@@ -1193,30 +1250,24 @@ int sse_walkers_create(sse_engine *e, int32_t model_id, int32_t count, const sse
     w.model = model_id;
     w.phase = PH_NEW;
     w.warmup = p.diagonal_warmup_sweeps;
-    e->walkers.push_back(h);
-    ids[i] = (int32_t)(first + i);
   }
   if (count)
     CUDA_TRY(e, cudaMemcpyAsync(e->d_walkers + first, dw.data(), sizeof(DevWalker) * count, cudaMemcpyHostToDevice,
                                 e->stream));
   CUDA_TRY(e, cudaStreamSynchronize(e->stream));
+  created.keep = true;
+  for (int i = 0; i < count; i++) ids[i] = (int32_t)(first + i);
   return SSE_OK;
 }
 
 int sse_walkers_destroy(sse_engine *e, int32_t count, const int32_t *ids) {
   if (!e || (count && !ids)) return SSE_ERR_ARG;
   cudaSetDevice(e->device);
+  const int crc = check_work_ids(e, count, ids);  // all known and distinct, or nothing is destroyed
+  if (crc) return crc;
   for (int i = 0; i < count; i++) {
-    if (!valid_id(e, ids[i])) return fail(e, SSE_ERR_ARG, "unknown walker id");
     HostWalker &h = e->walkers[ids[i]];
-    dev_free(e, h.ops);
-    dev_free(e, h.rec);
-    dev_free(e, h.cidx);
-    dev_free(e, h.vfirst);
-    dev_free(e, h.state);
-    dev_free(e, h.obs_sum);
-    dev_free(e, h.obs_last);
-    dev_free(e, h.obs_count);
+    free_walker_buffers(e, h);
     h.alive = false;
   }
   clear_graphs(e);

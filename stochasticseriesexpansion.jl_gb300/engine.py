@@ -99,57 +99,63 @@ _lib = None
 
 
 def lib():
+    """The engine library (libssegpu.so, built for sm_103a), loaded once."""
     global _lib
     if _lib is None:
         if not os.path.exists(LIB):
             raise RuntimeError(f"{LIB} is not built: run __graft_entry__.build() (nvcc, sm_103a)")
-        L = C.CDLL(LIB)
-        I32, I64, U32 = C.c_int32, C.c_int64, C.c_uint32
-        eng = C.c_void_p
-        sig = {
-            "sse_abi_version": ([], C.c_int),
-            "sse_engine_create": ([I32, P(eng)], C.c_int),
-            "sse_engine_destroy": ([eng], C.c_int),
-            "sse_engine_last_error": ([eng], C.c_char_p),
-            "sse_model_register": ([eng, P(ModelDesc), P(I32)], C.c_int),
-            "sse_model_nobs": ([eng, I32, P(I32)], C.c_int),
-            "sse_walkers_create": ([eng, I32, I32, P(WalkerParams), P(I32)], C.c_int),
-            "sse_walkers_destroy": ([eng, I32, P(I32)], C.c_int),
-            "sse_walkers_reserve": ([eng, I32, P(I32), I64], C.c_int),
-            "sse_walkers_init": ([eng, I32, P(I32)], C.c_int),
-            "sse_sweep": ([eng, I32, P(I32), I32, U32], C.c_int),
-            "sse_sweep_each": ([eng, I32, P(I32), P(I32), U32], C.c_int),
-            "sse_observables": ([eng, I32, P(I32), P(C.c_double), P(I64), P(C.c_double), I32], C.c_int),
-            "sse_walker_info_get": ([eng, I32, P(WalkerInfo)], C.c_int),
-            "sse_walker_export": ([eng, I32, P(U32), I64, P(C.c_uint8), P(WalkerInfo)], C.c_int),
-            "sse_walker_import": ([eng, I32, P(U32), P(C.c_uint8), P(WalkerInfo)], C.c_int),
-            "sse_vertex_list": ([eng, I32, P(I32), P(I32), P(I32)], C.c_int),
-            "sse_last_timing": ([eng, P(C.c_double), P(I64)], C.c_int),
-            "sse_set_launch": ([eng, I32, I32], C.c_int),
-            "sse_get_launch": ([eng, P(I32), P(I32)], C.c_int),
-            "sse_profiler_range": ([eng, I32], C.c_int),
-            "sse_autotune": ([eng, I32, P(I32), I32, U32, P(I32), P(I32), P(C.c_double)], C.c_int),
-            "sse_autotune_each": ([eng, I32, P(I32), P(I32), U32, P(I32), P(I32), P(C.c_double)], C.c_int),
-            "sse_set_staging": ([eng, I32], C.c_int),
-            "sse_get_staging": ([eng, P(I32)], C.c_int),
-            "sse_walker_set_T": ([eng, I32, C.c_double], C.c_int),
-            "sse_walkers_set_worm_cap": ([eng, I32, P(I32), I32], C.c_int),
-            "sse_check_walkers": ([eng, I32, P(I32), P(I32)], C.c_int),
-            "sse_tempering_exchange": ([eng, I32, I32, P(I32), C.c_uint64, C.c_uint64, P(I32)], C.c_int),
-            "sse_sweep_tempering": ([eng, I32, I32, P(I32), I32, I32, C.c_uint64, C.c_uint64, U32, P(I64), P(I64)],
-                                    C.c_int),
-            "sse_sweep_noalloc": ([P(ModelDesc), C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p, C.c_void_p,
-                                   C.c_void_p, I32, U32], C.c_int),
-        }
-        for name, (args, res) in sig.items():
-            f = getattr(L, name)
-            f.argtypes = args
-            f.restype = res
-        if L.sse_abi_version() != ABI_VERSION:
-            raise RuntimeError(f"{LIB} has ABI version {L.sse_abi_version()}, these bindings mirror version "
-                               f"{ABI_VERSION}: rebuild it with __graft_entry__.build()")
-        _lib = L
+        _lib = load_library(LIB)
     return _lib
+
+
+def load_library(path: str):
+    """Loads a build of the engine library from `path` and declares the C ABI's signatures on it."""
+    L = C.CDLL(path)
+    I32, I64, U32 = C.c_int32, C.c_int64, C.c_uint32
+    eng = C.c_void_p
+    sig = {
+        "sse_abi_version": ([], C.c_int),
+        "sse_engine_create": ([I32, P(eng)], C.c_int),
+        "sse_engine_destroy": ([eng], C.c_int),
+        "sse_engine_last_error": ([eng], C.c_char_p),
+        "sse_model_register": ([eng, P(ModelDesc), P(I32)], C.c_int),
+        "sse_model_nobs": ([eng, I32, P(I32)], C.c_int),
+        "sse_walkers_create": ([eng, I32, I32, P(WalkerParams), P(I32)], C.c_int),
+        "sse_walkers_destroy": ([eng, I32, P(I32)], C.c_int),
+        "sse_walkers_reserve": ([eng, I32, P(I32), I64], C.c_int),
+        "sse_walkers_init": ([eng, I32, P(I32)], C.c_int),
+        "sse_sweep": ([eng, I32, P(I32), I32, U32], C.c_int),
+        "sse_sweep_each": ([eng, I32, P(I32), P(I32), U32], C.c_int),
+        "sse_observables": ([eng, I32, P(I32), P(C.c_double), P(I64), P(C.c_double), I32], C.c_int),
+        "sse_walker_info_get": ([eng, I32, P(WalkerInfo)], C.c_int),
+        "sse_walker_export": ([eng, I32, P(U32), I64, P(C.c_uint8), P(WalkerInfo)], C.c_int),
+        "sse_walker_import": ([eng, I32, P(U32), P(C.c_uint8), P(WalkerInfo)], C.c_int),
+        "sse_vertex_list": ([eng, I32, P(I32), P(I32), P(I32)], C.c_int),
+        "sse_last_timing": ([eng, P(C.c_double), P(I64)], C.c_int),
+        "sse_set_launch": ([eng, I32, I32], C.c_int),
+        "sse_get_launch": ([eng, P(I32), P(I32)], C.c_int),
+        "sse_profiler_range": ([eng, I32], C.c_int),
+        "sse_autotune": ([eng, I32, P(I32), I32, U32, P(I32), P(I32), P(C.c_double)], C.c_int),
+        "sse_autotune_each": ([eng, I32, P(I32), P(I32), U32, P(I32), P(I32), P(C.c_double)], C.c_int),
+        "sse_set_staging": ([eng, I32], C.c_int),
+        "sse_get_staging": ([eng, P(I32)], C.c_int),
+        "sse_walker_set_T": ([eng, I32, C.c_double], C.c_int),
+        "sse_walkers_set_worm_cap": ([eng, I32, P(I32), I32], C.c_int),
+        "sse_check_walkers": ([eng, I32, P(I32), P(I32)], C.c_int),
+        "sse_tempering_exchange": ([eng, I32, I32, P(I32), C.c_uint64, C.c_uint64, P(I32)], C.c_int),
+        "sse_sweep_tempering": ([eng, I32, I32, P(I32), I32, I32, C.c_uint64, C.c_uint64, U32, P(I64), P(I64)],
+                                C.c_int),
+        "sse_sweep_noalloc": ([P(ModelDesc), C.c_void_p, C.c_void_p, I64, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.c_void_p, I32, U32], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    if L.sse_abi_version() != ABI_VERSION:
+        raise RuntimeError(f"{path} has ABI version {L.sse_abi_version()}, these bindings mirror version "
+                           f"{ABI_VERSION}: rebuild it with __graft_entry__.build()")
+    return L
 
 
 def exported_symbols():
@@ -221,8 +227,9 @@ def _ids(ids):
 class Engine:
     """One GPU, one stream, many walkers (see include/sse_gpu.h)."""
 
-    def __init__(self, device: int = 0):
-        self._L = lib()
+    def __init__(self, device: int = 0, library=None):
+        """`library`: a handle from load_library (default: the sm_103a build)."""
+        self._L = library if library is not None else lib()
         self.h = C.c_void_p()
         rc = self._L.sse_engine_create(device, C.byref(self.h))
         if rc != 0:

@@ -1,0 +1,183 @@
+// A stand-in for the CUDA runtime, linked into a test build of the engine library (nvcc
+// -cudart none) so that the C ABI's host paths -- allocation, validation, error returns and
+// clean-up -- run on a machine without a GPU.
+//
+// Device memory is host memory; copies and memsets act on it directly; kernel launches do
+// nothing (the device code is not run here: its results are checked on a GPU against the
+// oracle).  Test hooks count live allocations, catch frees of unknown pointers, and make the
+// k-th allocation from now fail with cudaErrorMemoryAllocation, as an out-of-memory device would.
+
+#include <cuda_profiler_api.h>
+#include <cuda_runtime_api.h>
+
+#include <cstdlib>
+#include <cstring>
+#include <map>
+
+namespace {
+std::map<void *, size_t> g_live;  // allocation -> bytes
+long g_fail_in = -1;              // allocations to go before one fails; -1: none
+long g_allocs = 0;                // allocations made
+long g_bad_frees = 0;             // frees of pointers that are not live
+long g_launches = 0;              // kernel launches (no-ops)
+char g_dummy[64];                 // backing for opaque handles (streams, events, pools)
+void *g_fatbin_handle[4];
+}  // namespace
+
+extern "C" {
+
+// ---- test hooks ----
+void fake_cuda_fail_alloc_in(long k) { g_fail_in = k; }
+long fake_cuda_live_allocs(void) { return (long)g_live.size(); }
+long fake_cuda_live_bytes(void) {
+  long b = 0;
+  for (auto &kv : g_live) b += (long)kv.second;
+  return b;
+}
+long fake_cuda_allocs(void) { return g_allocs; }
+long fake_cuda_bad_frees(void) { return g_bad_frees; }
+long fake_cuda_launches(void) { return g_launches; }
+
+// ---- memory ----
+cudaError_t cudaMallocAsync(void **p, size_t n, cudaStream_t) {
+  *p = nullptr;
+  if (g_fail_in == 0) {
+    g_fail_in = -1;
+    return cudaErrorMemoryAllocation;
+  }
+  if (g_fail_in > 0) g_fail_in--;
+  void *q = std::calloc(1, n ? n : 1);
+  if (!q) return cudaErrorMemoryAllocation;
+  g_live[q] = n;
+  g_allocs++;
+  *p = q;
+  return cudaSuccess;
+}
+
+cudaError_t cudaFreeAsync(void *p, cudaStream_t) {
+  if (!p) return cudaSuccess;
+  auto it = g_live.find(p);
+  if (it == g_live.end()) {
+    g_bad_frees++;
+    return cudaErrorInvalidValue;
+  }
+  std::free(p);
+  g_live.erase(it);
+  return cudaSuccess;
+}
+
+cudaError_t cudaMemcpy(void *dst, const void *src, size_t n, cudaMemcpyKind) {
+  if (n && (!dst || !src)) return cudaErrorInvalidValue;
+  if (n) std::memmove(dst, src, n);
+  return cudaSuccess;
+}
+
+cudaError_t cudaMemcpyAsync(void *dst, const void *src, size_t n, cudaMemcpyKind kind, cudaStream_t) {
+  return cudaMemcpy(dst, src, n, kind);
+}
+
+cudaError_t cudaMemsetAsync(void *p, int v, size_t n, cudaStream_t) {
+  if (n && !p) return cudaErrorInvalidValue;
+  if (n) std::memset(p, v, n);
+  return cudaSuccess;
+}
+
+// a __device__ variable's host shadow stands in for its device storage
+cudaError_t cudaGetSymbolAddress(void **p, const void *symbol) {
+  *p = const_cast<void *>(symbol);
+  return cudaSuccess;
+}
+
+cudaError_t cudaMemcpyFromSymbol(void *dst, const void *symbol, size_t n, size_t offset, cudaMemcpyKind) {
+  std::memmove(dst, static_cast<const char *>(symbol) + offset, n);
+  return cudaSuccess;
+}
+
+// ---- device, streams, events ----
+cudaError_t cudaGetDeviceCount(int *n) {
+  *n = 1;
+  return cudaSuccess;
+}
+cudaError_t cudaSetDevice(int d) { return d == 0 ? cudaSuccess : cudaErrorInvalidDevice; }
+cudaError_t cudaGetDevice(int *d) {
+  *d = 0;
+  return cudaSuccess;
+}
+cudaError_t cudaDeviceGetAttribute(int *v, cudaDeviceAttr attr, int) {
+  *v = attr == cudaDevAttrMultiProcessorCount ? 152 : 0;
+  return cudaSuccess;
+}
+cudaError_t cudaDeviceGetDefaultMemPool(cudaMemPool_t *pool, int) {
+  *pool = reinterpret_cast<cudaMemPool_t>(g_dummy);
+  return cudaSuccess;
+}
+cudaError_t cudaMemPoolSetAttribute(cudaMemPool_t, cudaMemPoolAttr, void *) { return cudaSuccess; }
+cudaError_t cudaStreamCreateWithFlags(cudaStream_t *s, unsigned int) {
+  *s = reinterpret_cast<cudaStream_t>(g_dummy + 8);
+  return cudaSuccess;
+}
+cudaError_t cudaStreamDestroy(cudaStream_t) { return cudaSuccess; }
+cudaError_t cudaStreamSynchronize(cudaStream_t) { return cudaSuccess; }
+cudaError_t cudaEventCreate(cudaEvent_t *ev) {
+  *ev = reinterpret_cast<cudaEvent_t>(g_dummy + 16);
+  return cudaSuccess;
+}
+cudaError_t cudaEventRecord(cudaEvent_t, cudaStream_t) { return cudaSuccess; }
+cudaError_t cudaEventElapsedTime(float *ms, cudaEvent_t, cudaEvent_t) {
+  *ms = 0.001f;
+  return cudaSuccess;
+}
+cudaError_t cudaEventDestroy(cudaEvent_t) { return cudaSuccess; }
+cudaError_t cudaGetLastError(void) { return cudaSuccess; }
+const char *cudaGetErrorString(cudaError_t err) {
+  return err == cudaErrorMemoryAllocation ? "out of memory (fake runtime)" : "error (fake runtime)";
+}
+cudaError_t cudaProfilerStart(void) { return cudaSuccess; }
+cudaError_t cudaProfilerStop(void) { return cudaSuccess; }
+
+// ---- kernels: launch configuration accepted, nothing runs ----
+cudaError_t cudaFuncSetAttribute(const void *, cudaFuncAttribute, int) { return cudaSuccess; }
+cudaError_t cudaOccupancyMaxActiveBlocksPerMultiprocessor(int *n, const void *, int, size_t) {
+  *n = 8;
+  return cudaSuccess;
+}
+
+// ---- CUDA graphs: not offered (callers get an error, as from a device without graph support) ----
+cudaError_t cudaStreamBeginCapture(cudaStream_t, cudaStreamCaptureMode) { return cudaErrorNotSupported; }
+cudaError_t cudaStreamEndCapture(cudaStream_t, cudaGraph_t *g) {
+  *g = nullptr;
+  return cudaErrorNotSupported;
+}
+cudaError_t cudaGraphInstantiate(cudaGraphExec_t *x, cudaGraph_t, unsigned long long) {
+  *x = nullptr;
+  return cudaErrorNotSupported;
+}
+cudaError_t cudaGraphLaunch(cudaGraphExec_t, cudaStream_t) { return cudaErrorNotSupported; }
+cudaError_t cudaGraphExecDestroy(cudaGraphExec_t) { return cudaSuccess; }
+cudaError_t cudaGraphDestroy(cudaGraph_t) { return cudaSuccess; }
+
+// ---- what nvcc's generated host code calls at load time and for <<<...>>> ----
+void **__cudaRegisterFatBinary(void *) { return g_fatbin_handle; }
+void __cudaRegisterFatBinaryEnd(void **) {}
+void __cudaUnregisterFatBinary(void **) {}
+void __cudaRegisterFunction(void **, const char *, char *, const char *, int, uint3 *, uint3 *, dim3 *, dim3 *,
+                            int *) {}
+void __cudaRegisterVar(void **, char *, char *, const char *, int, size_t, int, int) {}
+unsigned __cudaPushCallConfiguration(dim3, dim3, size_t, struct CUstream_st *) { return 0; }
+cudaError_t __cudaPopCallConfiguration(dim3 *grid, dim3 *block, size_t *shared, void *stream) {
+  *grid = dim3(1, 1, 1);
+  *block = dim3(1, 1, 1);
+  *shared = 0;
+  *static_cast<cudaStream_t *>(stream) = nullptr;
+  return cudaSuccess;
+}
+cudaError_t __cudaGetKernel(cudaKernel_t *k, const void *fn) {
+  *k = reinterpret_cast<cudaKernel_t>(const_cast<void *>(fn));
+  return cudaSuccess;
+}
+cudaError_t __cudaLaunchKernel(cudaKernel_t, dim3, dim3, void **, size_t, cudaStream_t) {
+  g_launches++;
+  return cudaSuccess;
+}
+
+}  // extern "C"
