@@ -28,3 +28,26 @@ def O():
 
     oracle.lib()
     return oracle
+
+
+@pytest.fixture(scope="session")
+def fake():
+    """The engine library built against the fake CUDA runtime of tests/fake_cuda (no GPU needed),
+    with its test hooks declared."""
+    import ctypes as C
+    import shutil
+
+    if shutil.which("nvcc") is None:
+        pytest.skip("nvcc unavailable")
+    sys.path.insert(0, os.path.join(ROOT, "tests", "fake_cuda"))
+    try:
+        import build as fake_build
+    finally:
+        sys.path.pop(0)
+    from sse_gb300.engine import load_library
+
+    L = load_library(fake_build.build())
+    for name in ("fake_cuda_live_allocs", "fake_cuda_allocs", "fake_cuda_bad_frees", "fake_cuda_launches"):
+        getattr(L, name).restype = C.c_long
+    L.fake_cuda_fail_alloc_in.argtypes = [C.c_long]
+    return L
