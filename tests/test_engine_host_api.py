@@ -161,3 +161,44 @@ def test_tempering_ladder_checks(S, eng):
         eng.tempering_exchange(np.array([[w1[0]]], dtype=np.int32), seed=1, step=0)
     acc = eng.tempering_exchange(np.array([[w1[0], w1[1]], [w1[2], w1[3]]], dtype=np.int32), seed=1, step=0)
     assert acc.shape == (2, 1)
+
+
+def test_noalloc_argument_and_limit_checks(S, fake):
+    """sse_sweep_noalloc refuses null buffers and a negative sweep count (SSE_ERR_ARG) and sizes
+    beyond its static scratch (SSE_ERR_CAPACITY) before it launches anything.  On the fake runtime
+    device addresses are host addresses, so numpy buffers stand in for the caller's device memory."""
+    import ctypes as C
+
+    from sse_gb300.engine import SSE_SWEEP_MEASURE, NoAllocWalker, device_model_desc
+
+    CAPACITY = 3
+    flat = square(S, 4)
+    keep = {}
+
+    def dev(name, arr):
+        keep[name] = np.ascontiguousarray(arr)
+        return keep[name].ctypes.data
+
+    desc = device_model_desc(flat, dev)
+    walker = NoAllocWalker(T=0.5, seed=1, stream=0, init_opstring_cutoff=-1, diagonal_warmup_sweeps=5,
+                           init_num_worms=5.0, num_worms_attenuation_factor=0.01, target_worm_length_fraction=2.0)
+    ops = np.zeros(256, dtype=np.uint32)
+    state = np.zeros(flat.nsites, dtype=np.uint8)
+    nobs = 6 + 5 * flat.nest
+    obs_sum, obs_last, obs_count = np.zeros(nobs), np.zeros(nobs), np.zeros(nobs, dtype=np.int64)
+
+    def call(d=desc, w=C.addressof(walker), o=ops.ctypes.data, cap=len(ops), s=state.ctypes.data, n=1):
+        return fake.sse_sweep_noalloc(C.byref(d), C.c_void_p(w), C.c_void_p(o), cap, C.c_void_p(s),
+                                      C.c_void_p(obs_sum.ctypes.data), C.c_void_p(obs_count.ctypes.data),
+                                      C.c_void_p(obs_last.ctypes.data), n, SSE_SWEEP_MEASURE)
+
+    launches0 = fake.fake_cuda_launches()
+    assert call(w=None) == ARG and call(o=None) == ARG and call(s=None) == ARG and call(n=-1) == ARG
+    assert call(cap=0) == CAPACITY and call(cap=(1 << 18) + 1) == CAPACITY
+    for field, value, code in (("nsites", (1 << 14) + 1, CAPACITY), ("nbonds", (1 << 16) + 1, CAPACITY),
+                               ("ntypes", 65, CAPACITY), ("maxdim", 1, ARG), ("nest", -1, ARG)):
+        d = device_model_desc(flat, dev)
+        setattr(d, field, value)
+        assert call(d=d) == code, field
+    assert fake.fake_cuda_launches() == launches0
+    assert call() == 0 and fake.fake_cuda_launches() > launches0
