@@ -29,6 +29,7 @@
 
 using namespace sse;
 
+// ==== kernels: begin (device code only down to the matching end marker) ====
 namespace {
 
 constexpr int MODE_INIT = 0;
@@ -434,6 +435,7 @@ __global__ void __launch_bounds__(256) k_tempering(DevWalker *walkers, const Dev
 }
 
 }  // namespace
+// ==== kernels: end ====
 
 // ---------------------------------------------------------------------------
 // host engine

@@ -2,9 +2,9 @@
 // -cudart none) so that the C ABI's host paths -- allocation, validation, error returns and
 // clean-up -- run on a machine without a GPU.
 //
-// Device memory is host memory; copies and memsets act on it directly; kernel launches do
-// nothing (the device code is not run here: its results are checked on a GPU against the
-// oracle).  Test hooks count live allocations, catch frees of unknown pointers, and make the
+// Device memory is host memory; copies and memsets act on it directly.  A kernel launch does
+// nothing, unless the library also links the warp emulator of tests/warp_emu, which defines
+// emu_dispatch: then the launch runs a host build of the same kernel on emulated warps.  Test hooks count live allocations, catch frees of unknown pointers, and make the
 // k-th allocation from now fail with cudaErrorMemoryAllocation, as an out-of-memory device would.
 
 #include <cuda_profiler_api.h>
@@ -13,13 +13,20 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <string>
 
 namespace {
 std::map<void *, size_t> g_live;  // allocation -> bytes
 long g_fail_in = -1;              // allocations to go before one fails; -1: none
 long g_allocs = 0;                // allocations made
 long g_bad_frees = 0;             // frees of pointers that are not live
-long g_launches = 0;              // kernel launches (no-ops)
+long g_launches = 0;              // kernel launches
+// host stub -> device (mangled) name; filled by the registration constructors of the engine's
+// object, which may run before this file's globals are constructed, hence constructed on first use
+std::map<const void *, std::string> &kernel_names() {
+  static std::map<const void *, std::string> names;
+  return names;
+}
 char g_dummy[64];                 // backing for opaque handles (streams, events, pools)
 void *g_fatbin_handle[4];
 }  // namespace
@@ -129,7 +136,10 @@ cudaError_t cudaEventElapsedTime(float *ms, cudaEvent_t, cudaEvent_t) {
 }
 cudaError_t cudaEventDestroy(cudaEvent_t) { return cudaSuccess; }
 cudaError_t cudaGetLastError(void) { return cudaSuccess; }
+const char *emu_last_failure(void) __attribute__((weak));  // tests/warp_emu: why a launch failed
+
 const char *cudaGetErrorString(cudaError_t err) {
+  if (err == cudaErrorLaunchFailure && emu_last_failure) return emu_last_failure();
   return err == cudaErrorMemoryAllocation ? "out of memory (fake runtime)" : "error (fake runtime)";
 }
 cudaError_t cudaProfilerStart(void) { return cudaSuccess; }
@@ -160,24 +170,45 @@ cudaError_t cudaGraphDestroy(cudaGraph_t) { return cudaSuccess; }
 void **__cudaRegisterFatBinary(void *) { return g_fatbin_handle; }
 void __cudaRegisterFatBinaryEnd(void **) {}
 void __cudaUnregisterFatBinary(void **) {}
-void __cudaRegisterFunction(void **, const char *, char *, const char *, int, uint3 *, uint3 *, dim3 *, dim3 *,
-                            int *) {}
+void __cudaRegisterFunction(void **, const char *host_fun, char *, const char *device_name, int, uint3 *, uint3 *,
+                            dim3 *, dim3 *, int *) {
+  kernel_names()[host_fun] = device_name;
+}
 void __cudaRegisterVar(void **, char *, char *, const char *, int, size_t, int, int) {}
-unsigned __cudaPushCallConfiguration(dim3, dim3, size_t, struct CUstream_st *) { return 0; }
+// <<<grid, block, shared, stream>>> pushes the configuration; the launch stub pops it again
+struct LaunchConfig {
+  dim3 grid, block;
+  size_t shared;
+  cudaStream_t stream;
+};
+LaunchConfig g_config;
+unsigned __cudaPushCallConfiguration(dim3 grid, dim3 block, size_t shared, struct CUstream_st *stream) {
+  g_config = LaunchConfig{grid, block, shared, stream};
+  return 0;
+}
 cudaError_t __cudaPopCallConfiguration(dim3 *grid, dim3 *block, size_t *shared, void *stream) {
-  *grid = dim3(1, 1, 1);
-  *block = dim3(1, 1, 1);
-  *shared = 0;
-  *static_cast<cudaStream_t *>(stream) = nullptr;
+  *grid = g_config.grid;
+  *block = g_config.block;
+  *shared = g_config.shared;
+  *static_cast<cudaStream_t *>(stream) = g_config.stream;
   return cudaSuccess;
 }
 cudaError_t __cudaGetKernel(cudaKernel_t *k, const void *fn) {
   *k = reinterpret_cast<cudaKernel_t>(const_cast<void *>(fn));
   return cudaSuccess;
 }
-cudaError_t __cudaLaunchKernel(cudaKernel_t, dim3, dim3, void **, size_t, cudaStream_t) {
+// defined by tests/warp_emu when it is linked in: runs the named kernel, 0 on success
+int emu_dispatch(const char *device_name, unsigned gx, unsigned gy, unsigned gz, unsigned bx, unsigned by,
+                 unsigned bz, size_t smem, void **args) __attribute__((weak));
+
+cudaError_t __cudaLaunchKernel(cudaKernel_t kernel, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t) {
   g_launches++;
-  return cudaSuccess;
+  if (!emu_dispatch) return cudaSuccess;
+  auto it = kernel_names().find(reinterpret_cast<const void *>(kernel));
+  if (it == kernel_names().end()) return cudaErrorInvalidDeviceFunction;
+  return emu_dispatch(it->second.c_str(), grid.x, grid.y, grid.z, block.x, block.y, block.z, smem, args) == 0
+             ? cudaSuccess
+             : cudaErrorLaunchFailure;
 }
 
 }  // extern "C"

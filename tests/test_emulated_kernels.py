@@ -1,0 +1,191 @@
+"""The engine's own kernels, run on the CPU on emulated warps (tests/warp_emu), against the oracle.
+
+The emulated library is built from the engine's device sources with three textual substitutions
+(two PTX statements and the dynamic shared-memory declaration; see tests/warp_emu/build.py).  It
+runs every launch of the C ABI's host code, with the fake CUDA runtime of tests/fake_cuda as device
+memory.  So these tests check the kernels' logic, bit for bit against the oracle, without a GPU:
+the diagonal update, linking, worms, the controller, measurement, cutoff growth, staging, the plain
+and cost-balanced paths, tempering, the invariant check and the worm cap.  What they cannot check
+is what only the hardware does: the compiled sm_103a code, memory ordering between warps, timing.
+The GPU tests (-m gpu) check those, with the same oracle.
+"""
+
+import numpy as np
+import pytest
+
+from golden_cases import CASES
+
+
+@pytest.fixture
+def eng(emu):
+    from sse_gb300.engine import Engine
+
+    e = Engine(0, library=emu)
+    yield e
+    e.close()
+
+
+def compare(eng, flat, wid, w, measured=True, counters=True):
+    """Engine walker `wid` against oracle walker `w`: everything bit for bit (`counters`: also the
+    cumulative worm-step count, a diagnostic that an imported walker starts afresh)."""
+    ops, st, inf = eng.export(int(wid))
+    assert inf["status"] == w.w.status
+    assert inf["L"] == w.w.L and inf["num_operators"] == w.w.num_operators and inf["sweeps"] == w.w.sweeps
+    assert inf["rng_counter"] == w.w.ctr
+    assert inf["num_worms"] == w.w.num_worms and inf["avg_worm_length"] == w.w.avg_worm_length
+    if counters:
+        assert inf["worm_steps"] == w.w.worm_steps_total
+    assert np.array_equal(ops, w.ops) and np.array_equal(st, w.state)
+    if measured:
+        s, c, _ = eng.observables([int(wid)])[0]
+        so, co, _ = w.obs()
+        assert np.array_equal(c, co)
+        np.testing.assert_array_equal(s, so)
+
+
+@pytest.mark.parametrize("case", list(CASES)[:4])
+def test_emulated_sweeps_match_oracle(S, O, eng, case):
+    """The golden cases' model families (S=1/2 square, mixed-spin honeycomb, S=1 bilayer with field
+    and anisotropy, the dimer cluster model), two chains each plus one grown from a zero cutoff."""
+    c = CASES[case]
+    flat = S.flatten_model(c["model"](S))
+    mid = eng.register_model(flat)
+    streams = list(c["streams"]) + [99]
+    params = [dict(T=c["T"], seed=c["seed"], stream=s, thermalization=c["therm"],
+                   init_opstring_cutoff=0 if s == 99 else -1) for s in streams]
+    ids = eng.create_walkers(mid, params)
+    eng.init(ids)
+    eng.sweep(ids, c["therm"] + 6, measure=True)
+    om = O.OracleModel(flat)
+    for p, wid in zip(params, ids.tolist()):
+        w = O.OracleWalker(om, T=p["T"], seed=p["seed"], stream=p["stream"], thermalization=p["thermalization"])
+        w.init(init_cutoff=p["init_opstring_cutoff"])
+        w.run(c["therm"] + 6, measure=True)
+        compare(eng, flat, wid, w)
+
+
+def square(S, side):
+    return S.flatten_model(S.MagnetModel({"lattice": {"unitcell": S.UnitCells.square, "size": (side, side)},
+                                          "J": 1.0, "measure": ["magnetization", "staggered_magnetization"]}))
+
+
+def oracle_after(O, flat, p, sweeps, init_cutoff=-1):
+    w = O.OracleWalker(O.OracleModel(flat), T=p["T"], seed=p["seed"], stream=p["stream"],
+                       thermalization=p.get("thermalization", 0))
+    w.init(init_cutoff=init_cutoff)
+    w.run(sweeps, measure=True)
+    return w
+
+
+@pytest.mark.parametrize("stage", [0, 4096, 192 * 1024])
+def test_emulated_launch_paths_match_oracle(S, O, eng, stage):
+    """Batched, one-launch-per-walker (plain) and cost-balanced (sse_sweep_each) launches, with the
+    worm update's records in global memory or staged in shared memory: the same chains."""
+    flat = square(S, 6)
+    mid = eng.register_model(flat)
+    params = [dict(T=0.25, seed=31, stream=k, thermalization=4) for k in range(3)]
+    ids = eng.create_walkers(mid, params)
+    eng.init(ids)
+    eng.set_staging(stage)
+    try:
+        eng.sweep(ids, 5, measure=True)
+        eng.sweep(ids[:2], 2, measure=True, plain=True)
+        eng.sweep_each(ids, [1, 3, 2], measure=True)
+    finally:
+        eng.set_staging(0)
+    for p, wid, n in zip(params, ids.tolist(), (8, 10, 7)):
+        compare(eng, flat, wid, oracle_after(O, flat, p, n))
+
+
+def test_emulated_export_import_continues_the_chain(S, O, eng):
+    """A walker exported mid-chain and imported into a fresh walker sweeps on exactly like the oracle."""
+    flat = square(S, 4)
+    mid = eng.register_model(flat)
+    p = dict(T=0.5, seed=41, stream=3, thermalization=2)
+    (a,) = eng.create_walkers(mid, [p]).tolist()
+    eng.init([a])
+    eng.sweep([a], 6, measure=True)
+    ops, st, inf = eng.export(a)
+    (b,) = eng.create_walkers(mid, [p]).tolist()
+    eng.import_(b, ops, st, inf)
+    eng.sweep([b], 5, measure=False)
+    w = oracle_after(O, flat, p, 6)
+    w.run(5, measure=False)
+    compare(eng, flat, b, w, measured=False, counters=False)
+
+
+def test_emulated_sweep_tempering_matches_oracle(S, O, eng):
+    """Blocks of Carlo steps with device exchange steps between them (k_tempering): accept counts,
+    temperatures and the accumulators that move with them, as the oracle's exchange gives them."""
+    flat = square(S, 4)
+    mid = eng.register_model(flat)
+    temps, nl, seed = [0.3, 0.45, 0.7, 1.1, 1.7], 3, 41
+    nr = len(temps)
+    params = [dict(T=temps[k], seed=seed, stream=l * nr + k, thermalization=3) for l in range(nl) for k in range(nr)]
+    ids = eng.create_walkers(mid, params).reshape(nl, nr)
+    eng.init(ids.ravel())
+    om = O.OracleModel(flat)
+    ws = []
+    for p in params:
+        w = O.OracleWalker(om, T=p["T"], seed=seed, stream=p["stream"], thermalization=3)
+        w.init()
+        ws.append(w)
+    nblocks, interval = 10, 3
+    acc, prop = eng.sweep_tempering(ids, nblocks, interval, seed=77, first_step=5, measure=True)
+    acc_o, prop_o = np.zeros_like(acc), np.zeros_like(prop)
+    for b in range(nblocks):
+        for w in ws:
+            w.run(interval, measure=True)
+        a, rc = O.tempering_exchange(ws, nl, nr, seed=77, step=5 + b)
+        assert rc == 0
+        acc_o += a == 1
+        prop_o += a >= 0
+    assert np.array_equal(acc, acc_o) and np.array_equal(prop, prop_o) and acc.sum() > 0
+    for wid, w in zip(ids.ravel().tolist(), ws):
+        assert eng.info(wid)["T"] == w.w.T
+        compare(eng, flat, wid, w)
+
+
+def test_emulated_invariant_check_finds_planted_inconsistency(S, O, eng):
+    """k_check passes consistent walkers and reports a spin flipped against the opstring."""
+    import sse_gb300.util as U
+
+    flat = square(S, 4)
+    mid = eng.register_model(flat)
+    a, b = eng.create_walkers(mid, [dict(T=0.5, seed=2, stream=k) for k in range(2)]).tolist()
+    eng.init([a, b])
+    eng.sweep([a, b], 4)
+    assert eng.check([a, b]).tolist() == [0, 0]
+    ops, st, inf = eng.export(b)
+    site = int(flat.arrays["bond_sites"][2 * U.dev_get_bond(int(ops[np.flatnonzero(ops)[0]]))])
+    st = st.copy()
+    st[site] ^= 1
+    eng.import_(b, ops, st, inf)
+    res = eng.check([a, b]).tolist()
+    assert res[0] == 0 and res[1] in (4, 5)
+
+
+def test_emulated_worm_cap_matches_oracle(S, O, eng):
+    """The long worm of the S=1 bilayer pinned in test_worm_cap.py: the engine's kernels stop the
+    walker where the oracle does, with the same opstring and replay counter, while the other walker
+    of the launch completes its sweeps."""
+    from sse_gb300.engine import SSEError
+    from test_worm_cap import LONG_WORM, long_worm_model
+
+    flat = long_worm_model(S)
+    mid = eng.register_model(flat)
+    therm = 100
+    params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=therm)
+              for s in (LONG_WORM["stream"], 0)]
+    ids = eng.create_walkers(mid, params)
+    eng.init(ids)
+    with pytest.raises(SSEError) as err:
+        eng.sweep(ids, 3, measure=False)
+    assert err.value.code == 8
+    w = O.OracleWalker(O.OracleModel(flat), T=params[0]["T"], seed=params[0]["seed"], stream=params[0]["stream"],
+                       thermalization=therm)
+    w.init()
+    with pytest.raises(RuntimeError):
+        w.run(3, measure=False)
+    compare(eng, flat, int(ids[0]), w, measured=False)
+    assert eng.info(int(ids[1]))["sweeps"] == 3 and eng.info(int(ids[1]))["status"] == 0

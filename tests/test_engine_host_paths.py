@@ -9,34 +9,10 @@ already uploaded.  The device code itself is checked on a GPU against the oracle
 runs.
 """
 
-import ctypes as C
-import shutil
-
 import numpy as np
 import pytest
 
 NOMEM, ARG = 6, 1
-
-
-@pytest.fixture(scope="module")
-def fake():
-    if shutil.which("nvcc") is None:
-        pytest.skip("nvcc unavailable")
-    import os
-    import sys
-
-    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "fake_cuda"))
-    try:
-        import build as fake_build
-    finally:
-        sys.path.pop(0)
-    from sse_gb300.engine import load_library
-
-    L = load_library(fake_build.build())
-    for name in ("fake_cuda_live_allocs", "fake_cuda_allocs", "fake_cuda_bad_frees", "fake_cuda_launches"):
-        getattr(L, name).restype = C.c_long
-    L.fake_cuda_fail_alloc_in.argtypes = [C.c_long]
-    return L
 
 
 @pytest.fixture
