@@ -165,17 +165,16 @@ def test_emulated_invariant_check_finds_planted_inconsistency(S, O, eng):
     assert res[0] == 0 and res[1] in (4, 5)
 
 
-def test_emulated_worm_cap_matches_oracle(S, O, eng):
-    """The long worm of the S=1 bilayer pinned in test_worm_cap.py: the engine's kernels stop the
-    walker where the oracle does, with the same opstring and replay counter, while the other walker
-    of the launch completes its sweeps."""
+def test_emulated_worm_cap_stop_matches_oracle(S, O, eng):
+    """The long worm of the S=1 bilayer pinned in test_worm_cap.py, in a measured sweep: the
+    engine's kernels stop the walker where the oracle does, with the same opstring and replay
+    counter, while the other walker of the launch completes its sweeps."""
     from sse_gb300.engine import SSEError
-    from test_worm_cap import LONG_WORM, long_worm_model
+    from test_worm_cap import LONG_WORM, MEASURED, long_worm_model
 
     flat = long_worm_model(S)
     mid = eng.register_model(flat)
-    therm = 100
-    params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=therm)
+    params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=MEASURED)
               for s in (LONG_WORM["stream"], 0)]
     ids = eng.create_walkers(mid, params)
     eng.init(ids)
@@ -183,9 +182,39 @@ def test_emulated_worm_cap_matches_oracle(S, O, eng):
         eng.sweep(ids, 3, measure=False)
     assert err.value.code == 8
     w = O.OracleWalker(O.OracleModel(flat), T=params[0]["T"], seed=params[0]["seed"], stream=params[0]["stream"],
-                       thermalization=therm)
+                       thermalization=MEASURED)
     w.init()
     with pytest.raises(RuntimeError):
         w.run(3, measure=False)
     compare(eng, flat, int(ids[0]), w, measured=False)
+    assert eng.info(int(ids[0]))["worm_undos"] == 0
     assert eng.info(int(ids[1]))["sweeps"] == 3 and eng.info(int(ids[1]))["status"] == 0
+
+
+@pytest.mark.parametrize("stage", [0, 192 * 1024])
+def test_emulated_worm_cap_undo_matches_oracle(S, O, eng, stage):
+    """The same worm in a thermalisation sweep: the kernels undo the sweep's worm phase exactly as
+    the oracle does (records in global memory, and staged in shared memory), and the walker sweeps
+    on bit for bit."""
+    from test_worm_cap import LONG_WORM, THERMALISING, long_worm_model
+
+    flat = long_worm_model(S)
+    mid = eng.register_model(flat)
+    params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=THERMALISING)
+              for s in (LONG_WORM["stream"], 0)]
+    ids = eng.create_walkers(mid, params)
+    eng.init(ids)
+    eng.set_staging(stage)
+    try:
+        eng.sweep(ids, 5, measure=False)
+    finally:
+        eng.set_staging(0)
+    om = O.OracleModel(flat)
+    for p, wid in zip(params, ids.tolist()):
+        w = O.OracleWalker(om, T=p["T"], seed=p["seed"], stream=p["stream"], thermalization=THERMALISING)
+        w.init()
+        w.run(5, measure=False)
+        compare(eng, flat, wid, w, measured=False)
+        assert eng.info(wid)["worm_undos"] == w.w.worm_undos
+    assert eng.info(int(ids[0]))["worm_undos"] == 1
+    assert eng.check(ids).tolist() == [0, 0]
