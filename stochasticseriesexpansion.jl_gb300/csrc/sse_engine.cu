@@ -1822,6 +1822,7 @@ int sse_sweep_tempering(sse_engine *e, int32_t nladders, int32_t nrungs, const i
 
 namespace {
 
+// ==== noalloc kernels: begin (device code only down to the matching end marker) ====
 struct NoAllocScratch {
   Rec rec[SSE_NOALLOC_MAX_SLOTS];
   int32_t cidx[SSE_NOALLOC_MAX_SLOTS];
@@ -2105,6 +2106,7 @@ __global__ void k_noalloc_finish(NoAllocScratch *X, sse_noalloc_walker *uw) {
   X->status = st;
 }
 
+// ==== noalloc kernels: end ====
 void *g_noalloc_ptr[64];
 bool g_noalloc_ready[64];
 

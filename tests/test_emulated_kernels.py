@@ -218,3 +218,60 @@ def test_emulated_worm_cap_undo_matches_oracle(S, O, eng, stage):
         assert eng.info(wid)["worm_undos"] == w.w.worm_undos
     assert eng.info(int(ids[0]))["worm_undos"] == 1
     assert eng.check(ids).tolist() == [0, 0]
+
+
+def test_emulated_noalloc_matches_oracle(S, O, emu):
+    """The allocation-free entry point (k_noalloc_prep, k_walk on its static scratch,
+    k_noalloc_finish) against the oracle: two calls of 4 Carlo steps each, the first with an opstring
+    buffer too small for the cutoff growth, which returns SSE_ERR_CAPACITY with the size needed and
+    resumes when called again with a larger buffer.  On the emulated runtime device addresses are
+    host addresses, so numpy buffers are the caller's device memory."""
+    import ctypes as C
+
+    from sse_gb300.engine import SSE_SWEEP_MEASURE, NoAllocWalker, device_model_desc
+
+    flat = S.flatten_model(S.MagnetModel({"lattice": {"unitcell": S.UnitCells.square, "size": (8, 8)},
+                                          "J": 1.0, "measure": ["magnetization", "staggered_magnetization"]}))
+    params = dict(T=0.5, seed=4242, stream=17, thermalization=2)
+    keep = {}
+
+    def dev(name, arr):
+        keep[name] = np.ascontiguousarray(arr).copy()
+        return keep[name].ctypes.data
+
+    desc = device_model_desc(flat, dev)
+    w = NoAllocWalker(T=params["T"], seed=params["seed"], stream=params["stream"], init_opstring_cutoff=-1,
+                      diagonal_warmup_sweeps=5, phase=0, init_num_worms=5.0, num_worms_attenuation_factor=0.01,
+                      target_worm_length_fraction=2.0, thermalization=params["thermalization"])
+    nobs = 6 + 5 * flat.nest
+    state = np.zeros(flat.nsites, dtype=np.uint8)
+    osum, ocnt, olast = np.zeros(nobs), np.zeros(nobs, dtype=np.int64), np.zeros(nobs)
+
+    def call(ops, nsweeps):
+        return emu.sse_sweep_noalloc(C.byref(desc), C.c_void_p(C.addressof(w)), C.c_void_p(ops.ctypes.data),
+                                     len(ops), C.c_void_p(state.ctypes.data), C.c_void_p(osum.ctypes.data),
+                                     C.c_void_p(ocnt.ctypes.data), C.c_void_p(olast.ctypes.data), nsweeps,
+                                     SSE_SWEEP_MEASURE)
+
+    ops = np.zeros(64, dtype=np.uint32)
+    rc = call(ops, 4)
+    grown = 0
+    while rc == 3:  # SSE_ERR_CAPACITY: the caller grows the opstring, keeping its prefix
+        assert w.need_capacity > len(ops)
+        bigger = np.zeros(w.need_capacity + 64, dtype=np.uint32)
+        bigger[: w.L] = ops[: w.L]
+        ops = bigger
+        grown += 1
+        rc = call(ops, 4 - (w.sweeps if w.phase == 2 else 0))
+    assert rc == 0 and grown > 0 and w.sweeps == 4
+    assert call(ops, 4) == 0
+    o = O.OracleWalker(O.OracleModel(flat), T=params["T"], seed=params["seed"], stream=params["stream"],
+                       thermalization=params["thermalization"])
+    o.init()
+    o.run(8, measure=True)
+    assert w.status == 0 and w.L == o.w.L and w.num_operators == o.w.num_operators and w.sweeps == 8
+    assert w.rng_counter == o.w.ctr and w.num_worms == o.w.num_worms and w.avg_worm_length == o.w.avg_worm_length
+    assert np.array_equal(ops[: w.L], o.ops) and np.array_equal(state, o.state)
+    so, co, _ = o.obs()
+    assert np.array_equal(ocnt, co)
+    np.testing.assert_array_equal(osum, so)

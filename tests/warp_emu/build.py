@@ -2,8 +2,8 @@
 tests/fake_cuda and a host build of the engine's own kernels running on emulated warps.
 
 The kernels are not copied or rewritten by hand.  They are taken from the engine's sources at build
-time: sse_device.cuh whole, and the block of sse_engine.cu between its "kernels: begin" and
-"kernels: end" markers.  Exactly three textual substitutions are applied, each checked to occur:
+time: sse_device.cuh whole, and the blocks of sse_engine.cu between its "kernels: begin" /
+"kernels: end" and "noalloc kernels: begin" / "noalloc kernels: end" markers.  Exactly three textual substitutions are applied, each checked to occur:
  - the PTX read of %lanemask_lt becomes the emulated lane mask;
  - the PTX L1 prefetch becomes a no-op;
  - the extern dynamic shared array becomes the emulated block's buffer.
@@ -29,6 +29,7 @@ KERNELS = {
     "k_walk<1>": "6k_walkILi1E", "k_walk<0>": "6k_walkILi0E", "k_set_targets": "13k_set_targets",
     "k_apply_growth": "14k_apply_growth", "k_link_debug": "12k_link_debug", "k_gather_status": "15k_gather_status",
     "k_gather_obs": "12k_gather_obs", "k_check": "7k_check", "k_tempering": "11k_tempering",
+    "k_noalloc_prep": "14k_noalloc_prep", "k_noalloc_finish": "16k_noalloc_finish",
 }
 
 
@@ -51,6 +52,9 @@ def generate() -> str:
     begin = eng.index("// ==== kernels: begin")
     end = eng.index("// ==== kernels: end ====")
     block = eng[eng.index("\n", begin) + 1:end]
+    nb = eng.index("// ==== noalloc kernels: begin")
+    ne = eng.index("// ==== noalloc kernels: end ====")
+    block += "\nnamespace {\n" + eng[eng.index("\n", nb) + 1:ne] + "\n}  // namespace\n"
     block, n = re.subn(r"extern __shared__ __align__\(\d+\) uint8_t (\w+)\[\];",
                        r"uint8_t *\1 = static_cast<uint8_t *>(emu_dynamic_smem());", block)
     if n == 0 or "extern __shared__" in block:

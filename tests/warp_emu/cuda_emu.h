@@ -17,6 +17,7 @@
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
+#include <type_traits>
 
 #define __device__
 #define __global__
@@ -24,7 +25,7 @@
 #define __forceinline__ inline
 #define __noinline__ __attribute__((noinline))
 #define __restrict__ __restrict
-#define __align__(n) alignas(n)
+#define __align__(n) __attribute__((aligned(n)))
 #define __launch_bounds__(...)
 #define __shared__ static
 #define __constant__
@@ -119,6 +120,16 @@ inline int __any_sync(unsigned, int pred) { return (int)emu_collective(EMU_ANY, 
 inline void __syncwarp(unsigned = 0xFFFFFFFFu) { emu_collective(EMU_SYNC, 0, 0); }
 inline void __syncthreads() { emu_block_barrier(); }
 inline unsigned emu_lanemask_lt() { return (1u << emu_cur->lane) - 1u; }
+
+// device min/max (CUDA overloads them for integer arguments)
+template <class A, class B>
+inline std::common_type_t<A, B> max(A a, B b) {
+  return a > b ? a : b;
+}
+template <class A, class B>
+inline std::common_type_t<A, B> min(A a, B b) {
+  return a < b ? a : b;
+}
 
 inline int __popc(unsigned x) { return __builtin_popcount(x); }
 inline int __ffs(int x) { return __builtin_ffs(x); }
