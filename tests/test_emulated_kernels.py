@@ -275,3 +275,21 @@ def test_emulated_noalloc_matches_oracle(S, O, emu):
     so, co, _ = o.obs()
     assert np.array_equal(ocnt, co)
     np.testing.assert_array_equal(osum, so)
+
+
+def test_emulated_headline_size_walker_matches_oracle(S, O, eng):
+    """One walker of the benchmark workload at full size (32x32 S=1/2 Heisenberg, beta = 16,
+    L = 51,154 slots): 12 Carlo steps on emulated warps equal the oracle bit for bit."""
+    c = CASES["square32_beta16"]
+    flat = S.flatten_model(c["model"](S))
+    mid = eng.register_model(flat)
+    p = dict(T=c["T"], seed=c["seed"], stream=c["streams"][0], thermalization=c["therm"])
+    ids = eng.create_walkers(mid, [p])
+    eng.init(ids)
+    eng.sweep(ids, c["therm"] + c["sweeps"], measure=True)
+    w = O.OracleWalker(O.OracleModel(flat), T=p["T"], seed=p["seed"], stream=p["stream"],
+                       thermalization=p["thermalization"])
+    w.init()
+    w.run(c["therm"] + c["sweeps"], measure=True)
+    compare(eng, flat, int(ids[0]), w)
+    assert w.w.L > 50_000
