@@ -55,3 +55,21 @@ def test_bench_default_run_prints_the_contract_line(S, emu, monkeypatch, capsys)
     assert "workload" in line["config"]
     for key in ("sm_mhz", "sm_max_mhz", "reasons"):
         assert key in line["clocks"], key
+
+
+def test_smoke_runs_against_the_oracle(S, emu, monkeypatch):
+    """__graft_entry__.smoke() (4 walkers of the 8x8 model, init plus 6 Carlo steps, checked
+    against the oracle) completes on the emulated engine: its checks hold for the kernels' logic."""
+    import importlib.util
+    import os
+
+    import sse_gb300.engine as E
+
+    real_init = E.Engine.__init__
+    monkeypatch.setattr(E.Engine, "__init__",
+                        lambda self, device=0, library=None: real_init(self, device, library if library else emu))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("_entry_under_test", os.path.join(root, "__graft_entry__.py"))
+    entry = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(entry)
+    entry.smoke()
