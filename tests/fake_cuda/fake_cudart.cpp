@@ -13,7 +13,9 @@
 #include <cstdlib>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <string>
+#include <vector>
 
 namespace {
 std::map<void *, size_t> g_live;  // allocation -> bytes
@@ -28,6 +30,14 @@ std::map<const void *, std::string> &kernel_names() {
   return names;
 }
 char g_dummy[64];                 // backing for opaque handles (streams, events, pools)
+// a captured stream operation: a memset, or a kernel launch recorded by the warp emulator
+struct Op {
+  void *ptr = nullptr;
+  int value = 0;
+  size_t n = 0;
+  std::shared_ptr<void> launch;
+};
+std::vector<Op> *g_capture = nullptr;  // the stream capture in progress, if any
 void *g_fatbin_handle[4];
 }  // namespace
 
@@ -85,6 +95,14 @@ cudaError_t cudaMemcpyAsync(void *dst, const void *src, size_t n, cudaMemcpyKind
 
 cudaError_t cudaMemsetAsync(void *p, int v, size_t n, cudaStream_t) {
   if (n && !p) return cudaErrorInvalidValue;
+  if (g_capture) {
+    Op op;
+    op.ptr = p;
+    op.value = v;
+    op.n = n;
+    g_capture->push_back(op);
+    return cudaSuccess;
+  }
   if (n) std::memset(p, v, n);
   return cudaSuccess;
 }
@@ -152,19 +170,50 @@ cudaError_t cudaOccupancyMaxActiveBlocksPerMultiprocessor(int *n, const void *, 
   return cudaSuccess;
 }
 
-// ---- CUDA graphs: not offered (callers get an error, as from a device without graph support) ----
-cudaError_t cudaStreamBeginCapture(cudaStream_t, cudaStreamCaptureMode) { return cudaErrorNotSupported; }
+// ---- CUDA graphs: stream capture records memsets and launches, a graph launch replays them ----
+// (kernel launches are recorded only when the warp emulator is linked in: emu_capture)
+void *emu_capture(const char *device_name, unsigned gx, unsigned gy, unsigned gz, unsigned bx, unsigned by,
+                  unsigned bz, size_t smem, void **args) __attribute__((weak));
+int emu_replay(void *launch) __attribute__((weak));
+void emu_release(void *launch) __attribute__((weak));
+
+cudaError_t cudaStreamBeginCapture(cudaStream_t, cudaStreamCaptureMode) {
+  if (g_capture) return cudaErrorIllegalState;
+  g_capture = new std::vector<Op>();
+  return cudaSuccess;
+}
 cudaError_t cudaStreamEndCapture(cudaStream_t, cudaGraph_t *g) {
-  *g = nullptr;
-  return cudaErrorNotSupported;
+  if (!g_capture) {
+    *g = nullptr;
+    return cudaErrorIllegalState;
+  }
+  *g = reinterpret_cast<cudaGraph_t>(g_capture);
+  g_capture = nullptr;
+  return cudaSuccess;
 }
-cudaError_t cudaGraphInstantiate(cudaGraphExec_t *x, cudaGraph_t, unsigned long long) {
-  *x = nullptr;
-  return cudaErrorNotSupported;
+cudaError_t cudaGraphInstantiate(cudaGraphExec_t *x, cudaGraph_t g, unsigned long long) {
+  *x = reinterpret_cast<cudaGraphExec_t>(new std::vector<Op>(*reinterpret_cast<std::vector<Op> *>(g)));
+  return cudaSuccess;
 }
-cudaError_t cudaGraphLaunch(cudaGraphExec_t, cudaStream_t) { return cudaErrorNotSupported; }
-cudaError_t cudaGraphExecDestroy(cudaGraphExec_t) { return cudaSuccess; }
-cudaError_t cudaGraphDestroy(cudaGraph_t) { return cudaSuccess; }
+cudaError_t cudaGraphLaunch(cudaGraphExec_t x, cudaStream_t) {
+  for (const Op &op : *reinterpret_cast<std::vector<Op> *>(x)) {
+    if (!op.launch) {
+      if (op.n) std::memset(op.ptr, op.value, op.n);
+      continue;
+    }
+    g_launches++;
+    if (emu_replay && emu_replay(op.launch.get()) != 0) return cudaErrorLaunchFailure;
+  }
+  return cudaSuccess;
+}
+cudaError_t cudaGraphExecDestroy(cudaGraphExec_t x) {
+  delete reinterpret_cast<std::vector<Op> *>(x);
+  return cudaSuccess;
+}
+cudaError_t cudaGraphDestroy(cudaGraph_t g) {
+  delete reinterpret_cast<std::vector<Op> *>(g);
+  return cudaSuccess;
+}
 
 // ---- what nvcc's generated host code calls at load time and for <<<...>>> ----
 void **__cudaRegisterFatBinary(void *) { return g_fatbin_handle; }
@@ -202,9 +251,19 @@ int emu_dispatch(const char *device_name, unsigned gx, unsigned gy, unsigned gz,
                  unsigned bz, size_t smem, void **args) __attribute__((weak));
 
 cudaError_t __cudaLaunchKernel(cudaKernel_t kernel, dim3 grid, dim3 block, void **args, size_t smem, cudaStream_t) {
+  auto it = kernel_names().find(reinterpret_cast<const void *>(kernel));
+  if (g_capture) {
+    if (!emu_capture) return cudaSuccess;  // nothing runs without the emulator, so nothing to record
+    if (it == kernel_names().end()) return cudaErrorInvalidDeviceFunction;
+    void *launch = emu_capture(it->second.c_str(), grid.x, grid.y, grid.z, block.x, block.y, block.z, smem, args);
+    if (!launch) return cudaErrorInvalidDeviceFunction;
+    Op op;
+    op.launch = std::shared_ptr<void>(launch, emu_release);
+    g_capture->push_back(op);
+    return cudaSuccess;
+  }
   g_launches++;
   if (!emu_dispatch) return cudaSuccess;
-  auto it = kernel_names().find(reinterpret_cast<const void *>(kernel));
   if (it == kernel_names().end()) return cudaErrorInvalidDeviceFunction;
   return emu_dispatch(it->second.c_str(), grid.x, grid.y, grid.z, block.x, block.y, block.z, smem, args) == 0
              ? cudaSuccess

@@ -293,3 +293,17 @@ def test_emulated_headline_size_walker_matches_oracle(S, O, eng):
     w.run(c["therm"] + c["sweeps"], measure=True)
     compare(eng, flat, int(ids[0]), w)
     assert w.w.L > 50_000
+
+
+def test_emulated_graph_replay_matches_oracle(S, O, eng):
+    """Sweep blocks captured once as a CUDA graph (flag and queue resets plus the persistent launch)
+    and replayed: the same chains as the oracle, block after block."""
+    flat = square(S, 6)
+    mid = eng.register_model(flat)
+    params = [dict(T=0.3, seed=51, stream=k, thermalization=3) for k in range(3)]
+    ids = eng.create_walkers(mid, params)
+    eng.init(ids)
+    for _ in range(3):  # the first call captures, the others replay the captured graph
+        eng.sweep(ids, 2, measure=True, graph=True)
+    for p, wid in zip(params, ids.tolist()):
+        compare(eng, flat, wid, oracle_after(O, flat, p, 6))

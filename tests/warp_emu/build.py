@@ -66,7 +66,7 @@ def generate() -> str:
     entries = " \\\n".join(f'  X("{needle}", {name})' for name, needle in KERNELS.items())
     return (
         "// Generated by tests/warp_emu/build.py from the engine's device sources.  Do not edit.\n"
-        "#include <cstring>\n#include <type_traits>\n#include <utility>\n\n"
+        "#include <cstring>\n#include <tuple>\n#include <type_traits>\n#include <utility>\n\n"
         '#include "cuda_emu.h"\n#define sse sse_emu\n' + dev + '\n#include "sse_gpu.h"\nusing namespace sse;\n'
         + block + "\n#define EMU_KERNELS(X) \\\n" + entries + "\n"
         '#include "emu_dispatch.inc"\n'

@@ -5,7 +5,6 @@ The results are NOT GPU results.  They say that each test's logic holds for the 
 run on emulated warps: the checks a test makes, the host code it drives, and the kernels'
 arithmetic against the oracle.  Whether the compiled sm_103a code does the same is what the real
 -m gpu run on a GB300 decides.  Not runnable here, and skipped by default:
- - tests that capture CUDA graphs (the fake runtime offers none);
  - tests whose buffers come from torch.cuda;
  - the full-size 4096-walker test and the statistical comparisons with exact diagonalisation
    (hours of emulated sweeps).
@@ -19,7 +18,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-SKIP = ("graph", "staging_matches_oracle", "test_gpu_fullsize", "test_zz_no_alloc", "_vs_ed", "matches_ed")
+SKIP = ("test_gpu_fullsize", "test_zz_no_alloc", "_vs_ed", "matches_ed")
 
 CHILD = r"""
 import os, sys
