@@ -381,6 +381,7 @@ def run_other_workload(args):
         line.update(config=desc, thermalization_sweeps=args.therm, thermalization_seconds=therm_s,
                     sweeps_per_step=args.sweeps_per_step, steps=args.steps, walker_sweeps_per_s=ws / t_dev,
                     operator_updates_per_s=ou / t_dev, walkers_stopped_by_worm_cap=failed,
+                    thermalisation_sweeps_undone_at_worm_cap=sum(info1[i]["worm_undos"] for i in ids.tolist()),
                     cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
     elif args.workload in ("magnet_bench", "cluster_bench"):
         line.update(run_reference_job(S, eng, args))
@@ -528,6 +529,7 @@ def run_reference_job(S, eng, args):
         config=desc, reference_task="2000 thermalisation + 5000 measured sweeps per walker",
         thermalization_sweeps=therm, measured_sweeps=sweeps, cpu_sample_sweeps=cpu_sweeps,
         walkers=nw, walkers_stopped_by_worm_cap=failed,
+        thermalisation_sweeps_undone_at_worm_cap=sum(info1[i]["worm_undos"] for i in ids.tolist()),
         gpu_batched_walker_sweeps_per_s=len(ids) * sweeps / meas_dev,
         gpu_batched_operator_updates_per_s=ou / meas_dev,
         gpu_batched_job_seconds_device=therm_dev + meas_dev, gpu_batched_job_seconds_wall=wall,

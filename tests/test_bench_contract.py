@@ -73,3 +73,32 @@ def test_smoke_runs_against_the_oracle(S, emu, monkeypatch):
     entry = importlib.util.module_from_spec(spec)
     spec.loader.exec_module(entry)
     entry.smoke()
+
+
+def test_reference_task_workload_prints_its_line(S, emu, monkeypatch, capsys):
+    """--workload magnet_bench (the reference's own benchmark task, batched) on two tiny walkers:
+    one JSON line with the batched, single-walker and CPU rates and the worm-cap accounting."""
+    import importlib.util
+    import os
+
+    import sse_gb300.engine as E
+
+    real_init = E.Engine.__init__
+    monkeypatch.setattr(E.Engine, "__init__",
+                        lambda self, device=0, library=None: real_init(self, device, library if library else emu))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    spec = importlib.util.spec_from_file_location("_bench_under_test2", os.path.join(root, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    monkeypatch.setattr("sys.argv", ["bench.py", "--workload", "magnet_bench", "--walkers", "2", "--therm", "5",
+                                     "--steps", "1", "--sweeps-per-step", "3", "--cpu-sweeps", "2",
+                                     "--cpu-threads", "2"])
+    bench.main()
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    line = json.loads(lines[0])
+    for key in ("workload", "walkers", "walkers_stopped_by_worm_cap", "thermalisation_sweeps_undone_at_worm_cap",
+                "gpu_batched_walker_sweeps_per_s", "gpu_single_walker_sweeps_per_s",
+                "cpu_oracle_all_cores_walker_sweeps_per_s"):
+        assert key in line, key
+    assert line["workload"] == "magnet_bench" and line["walkers"] == 2
