@@ -67,6 +67,7 @@ class Result:
     energy: float = float("nan")
     status: str = "ok"  # or the sse_status name that stopped one of its walkers
     replaced: int = 0  # walkers replaced by a fresh chain after the engine stopped them
+    undone: int = 0  # thermalisation sweeps whose worm phase was undone at the worm step cap
 
     @property
     def latency(self) -> float:
@@ -266,9 +267,11 @@ class ServingLoop:
             sums = np.array([o[0] for o in obs])
             counts = np.array([o[1] for o in obs])
             ou = a.spent_updates
+            undone = 0
             for i in a.ids.tolist():
                 inf = self.eng.info(i)
                 ou += inf["slot_visits"] + inf["worm_steps"]
+                undone += inf.get("worm_undos", 0)
             self.eng.destroy_walkers(a.ids)
             self.used -= a.nbytes
             mid, flat = self._model(a.req.model_key)
@@ -279,7 +282,7 @@ class ServingLoop:
             c = counts.sum(0)
             energy = (s[4] / c[4]) / (s[0] / c[0]) if (c[0] and c[4] and s[0]) else float("nan")
             res = Result(a.req.rid, a.req.arrival, t, names, sums, counts, ou, energy,
-                         status=failed.get(a.req.rid, "ok"), replaced=a.replaced)
+                         status=failed.get(a.req.rid, "ok"), replaced=a.replaced, undone=undone)
             self.results.append(res)
             out.append(res)
         return out
@@ -311,6 +314,7 @@ class ServingLoop:
             "requests": len(self.results),
             "failed": sum(r.status != "ok" for r in self.results),
             "walkers_replaced": sum(r.replaced for r in self.results),
+            "thermalisation_sweeps_undone": sum(r.undone for r in self.results),
             "p50_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "mean_s": float(lat.mean()) if len(lat) else None,
