@@ -46,7 +46,7 @@ typedef enum sse_status {
   SSE_ERR_TIMEOUT = 5,        /* a bounded device wait gave up */
   SSE_ERR_NOMEM = 6,          /* device or host allocation failed */
   SSE_ERR_STATE = 7,          /* call not valid in the walker's current state */
-  SSE_ERR_WORM_CAP = 8,       /* a worm exceeded the step cap (64 * (L + 16) unless set otherwise) */
+  SSE_ERR_WORM_CAP = 8,       /* a worm exceeded the step cap (64 * max(L + 16, 65536) unless set otherwise) */
   SSE_ERR_UNSUPPORTED = 9     /* model outside the engine's limits */
 } sse_status;
 
@@ -210,18 +210,19 @@ int sse_profiler_range(sse_engine *eng, int32_t start);
 int sse_check_walkers(sse_engine *eng, int32_t count, const int32_t *ids, int32_t *result);
 
 /* ---- worm step cap (no counterpart in the reference, whose worm_traverse! has no limit) ----
- * A worm that has not closed after factor * (L + 16) steps
+ * A worm that has not closed after factor * max(L + 16, 65536) steps
  *  - in a thermalisation sweep (sweeps <= thermalization) undoes the sweep's worm phase: the
  *    opstring returns to its state after the diagonal update, the worm-count controller and the
  *    spin state stay as they were, the draws the worms consumed stay consumed, worm_undos counts
  *    it, and the walker goes on (thermalisation sweeps need no detailed balance);
  *  - in a measured sweep stops its walker with SSE_ERR_WORM_CAP (the walker keeps that status;
  *    the other walkers go on).
- * The default factor is 64.  With S >= 1 and cluster-basis vertex tables, worms of the first
- * thermalisation sweeps (while L is still small) can run for orders of magnitude longer than the
- * opstring before they close, over 10^9 steps in some chains; the cap bounds how long one walker
- * holds up its batch.  After thermalisation worms rarely pass 64 * (L + 16) steps.  A smaller
- * factor undoes or stops such worms sooner and more often. */
+ * The default factor is 64, so the cap is at least about 4.2 million steps.  With S >= 1 and
+ * cluster-basis vertex tables, worms of the first thermalisation sweeps (while L is still small)
+ * can run for orders of magnitude longer than the opstring before they close, over 10^9 steps in
+ * some chains; the cap bounds how long one walker holds up its batch.  Small systems at low
+ * temperature run worms of hundreds of times L + 16 even after thermalisation, hence the minimum
+ * of 65536 slots.  A smaller factor undoes or stops long worms sooner and more often. */
 int sse_walkers_set_worm_cap(sse_engine *eng, int32_t count, const int32_t *ids, int32_t factor);
 
 /* ---- parallel tempering between resident walkers (src/sse.jl:390-405) ----

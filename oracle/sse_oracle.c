@@ -312,7 +312,7 @@ static int64_t worm_traverse(const orc_model *m, orc_walker *w) {
   int32_t leg_in = l0, wormfunc = wormfunc0;
   int64_t p = p0;
   int64_t worm_length = 1;
-  const int64_t cap = (int64_t)w->worm_cap_factor * (w->L + 16);
+  const int64_t cap = (int64_t)w->worm_cap_factor * (w->L + 16 > ORC_WORM_CAP_MIN_SLOTS ? w->L + 16 : ORC_WORM_CAP_MIN_SLOTS);
   for (;;) {
     uint32_t op = w->ops[p];
     uint32_t bond = op_bond(op);

@@ -92,7 +92,8 @@ typedef struct orc_walker {
   double *obs_sum;
   double *obs_last;
   int64_t *obs_count;
-  /* a worm stops the walker (ORC_ERR_WORM_CAP) after worm_cap_factor * (L + 16) steps; default 64.
+  /* a worm stops the walker (ORC_ERR_WORM_CAP) after worm_cap_factor * max(L + 16, ORC_WORM_CAP_MIN_SLOTS)
+   * steps; default 64.
    * During thermalisation the sweep's worm phase is undone instead: the opstring returns to its
    * state after the diagonal update, the controller and the spin state are left as they were,
    * and the walker goes on (no counterpart in the reference, whose worms have no limit). */
@@ -101,6 +102,9 @@ typedef struct orc_walker {
   uint32_t *ops_saved; /* the opstring before the worm phase, kept during thermalisation */
   int64_t ops_saved_cap;
 } orc_walker;
+
+/* the worm step cap counts at least this many opstring slots (small systems run long worms relative to L) */
+#define ORC_WORM_CAP_MIN_SLOTS 65536
 
 orc_walker *orc_walker_create(const orc_model *m, double T, uint64_t seed, uint64_t stream,
                               double init_num_worms, double attenuation, double target_fraction,

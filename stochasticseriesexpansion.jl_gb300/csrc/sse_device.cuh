@@ -29,6 +29,8 @@ constexpr int ST_INVALID_VERTEX = 4;
 constexpr int ST_TIMEOUT = 5;
 constexpr int ST_STATE = 7;
 constexpr int ST_WORM_CAP = 8;
+// a worm's step cap is cap_factor * max(L + 16, WORM_CAP_MIN_SLOTS)
+constexpr long long WORM_CAP_MIN_SLOTS = 1 << 16;
 // worm_update only: a thermalisation worm passed the step cap and the sweep's worm phase was
 // undone; the caller counts it and carries on with ST_OK (never stored in a walker)
 constexpr int ST_WORM_UNDONE = -8;
@@ -123,7 +125,7 @@ struct DevWalker {
   long long worm_undos;  // thermalisation worm phases undone at the step cap
   long long cyc[4];  // clock cycles spent in diagonal update, linking, worms, measurement
   int32_t model, status, phase, warmup, warmup_done;
-  int32_t cap_factor;  // a worm stops the walker after cap_factor * (L + 16) steps; 0: 64
+  int32_t cap_factor;  // worm step cap: cap_factor * max(L + 16, WORM_CAP_MIN_SLOTS); 0: 64
 };
 
 // ---------------------------------------------------------------------------
@@ -755,7 +757,9 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
   double total = 1.0;
   const double ceil_nw = ceil(wc.num_worms);
   const long long nworms = (long long)ceil_nw;
-  const long long cap = (long long)(cap_factor > 0 ? cap_factor : 64) * (c.L + 16);
+  // the cap counts at least WORM_CAP_MIN_SLOTS slots: small systems run long worms relative to L
+  const long long cap =
+      (long long)(cap_factor > 0 ? cap_factor : 64) * (c.L + 16 > WORM_CAP_MIN_SLOTS ? c.L + 16 : WORM_CAP_MIN_SLOTS);
   const unsigned long long L = (unsigned long long)c.L;
   for (long long wi = 0; wi < nworms; wi++) {
     if (c.n == 0) continue;  // worm_traverse! returns 0 without drawing

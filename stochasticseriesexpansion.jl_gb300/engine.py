@@ -418,7 +418,8 @@ class Engine:
         return out
 
     def set_worm_cap(self, ids, factor: int):
-        """Stop a walker when one of its worms exceeds factor * (L + 16) steps (default 64)."""
+        """Worm step cap factor (default 64): a worm longer than factor * max(L + 16, 65536) steps undoes
+        its thermalisation sweep's worm phase, or stops the walker in a measured sweep."""
         a, p = _ids(ids)
         self._check(self._L.sse_walkers_set_worm_cap(self.h, len(a), p, int(factor)))
 

@@ -84,3 +84,23 @@ def test_oracle_vs_ed(S, O, job, T):
         if z > 4:
             bad.append((name, mc, err, ref, z))
     assert not bad, bad
+
+
+@pytest.mark.parametrize("spin,size,T", [(1.5, (2, 3), 0.5), (2.0, (2, 2), 2.0)])
+def test_oracle_vs_ed_higher_spin(S, O, spin, size, T):
+    """Spins above 1 (site dimensions 4 and 5, with a field): the oracle's chains against exact
+    diagonalisation, |z| <= 4 on every observable."""
+    model = S.MagnetModel({"lattice": {"unitcell": S.UnitCells.square, "size": size}, "S": spin, "J": 1.0,
+                           "hz": 0.1, "measure": S.all_magnetization_estimators(2)})
+    flat = S.flatten_model(model)
+    assert flat.maxdim == int(2 * spin + 1)
+    ed = ed_observables(S, model, [T])
+    bins = run_binned(O, flat, T, seed=11, nbins=16, binsize=400, therm=1000)
+    bad = []
+    for name, f in evaluables(flat.est_prefixes, flat.norm_site_count).items():
+        mc, err = jackknife(bins, f)
+        ref = float(ed[name][0])
+        z = abs(mc - ref) / (err if err != 0 else 1e-8)
+        if z > 4:
+            bad.append((name, mc, err, ref, z))
+    assert not bad, bad

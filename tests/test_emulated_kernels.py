@@ -166,23 +166,25 @@ def test_emulated_invariant_check_finds_planted_inconsistency(S, O, eng):
 
 
 def test_emulated_worm_cap_stop_matches_oracle(S, O, eng):
-    """The long worm of the S=1 bilayer pinned in test_worm_cap.py, in a measured sweep: the
-    engine's kernels stop the walker where the oracle does, with the same opstring and replay
+    """The long worm of the S=1 bilayer pinned in test_worm_cap.py, in a measured sweep under the
+    lowered cap of that file: the engine's kernels stop the walker where the oracle does, with the same opstring and replay
     counter, while the other walker of the launch completes its sweeps."""
     from sse_gb300.engine import SSEError
-    from test_worm_cap import LONG_WORM, MEASURED, long_worm_model
+    from test_worm_cap import FACTOR, LONG_WORM, MEASURED, long_worm_model
 
     flat = long_worm_model(S)
     mid = eng.register_model(flat)
     params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=MEASURED)
               for s in (LONG_WORM["stream"], 0)]
     ids = eng.create_walkers(mid, params)
+    eng.set_worm_cap(ids, FACTOR)
     eng.init(ids)
     with pytest.raises(SSEError) as err:
         eng.sweep(ids, 3, measure=False)
     assert err.value.code == 8
     w = O.OracleWalker(O.OracleModel(flat), T=params[0]["T"], seed=params[0]["seed"], stream=params[0]["stream"],
                        thermalization=MEASURED)
+    w.w.worm_cap_factor = FACTOR
     w.init()
     with pytest.raises(RuntimeError):
         w.run(3, measure=False)
@@ -196,13 +198,14 @@ def test_emulated_worm_cap_undo_matches_oracle(S, O, eng, stage):
     """The same worm in a thermalisation sweep: the kernels undo the sweep's worm phase exactly as
     the oracle does (records in global memory, and staged in shared memory), and the walker sweeps
     on bit for bit."""
-    from test_worm_cap import LONG_WORM, THERMALISING, long_worm_model
+    from test_worm_cap import FACTOR, LONG_WORM, THERMALISING, long_worm_model
 
     flat = long_worm_model(S)
     mid = eng.register_model(flat)
     params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=THERMALISING)
               for s in (LONG_WORM["stream"], 0)]
     ids = eng.create_walkers(mid, params)
+    eng.set_worm_cap(ids, FACTOR)
     eng.init(ids)
     eng.set_staging(stage)
     try:
@@ -212,6 +215,7 @@ def test_emulated_worm_cap_undo_matches_oracle(S, O, eng, stage):
     om = O.OracleModel(flat)
     for p, wid in zip(params, ids.tolist()):
         w = O.OracleWalker(om, T=p["T"], seed=p["seed"], stream=p["stream"], thermalization=THERMALISING)
+        w.w.worm_cap_factor = FACTOR
         w.init()
         w.run(5, measure=False)
         compare(eng, flat, wid, w, measured=False)
@@ -307,3 +311,18 @@ def test_emulated_graph_replay_matches_oracle(S, O, eng):
         eng.sweep(ids, 2, measure=True, graph=True)
     for p, wid in zip(params, ids.tolist()):
         compare(eng, flat, wid, oracle_after(O, flat, p, 6))
+
+
+@pytest.mark.parametrize("spin,size", [(1.5, (2, 3)), (2.0, (2, 2))])
+def test_emulated_higher_spin_matches_oracle(S, O, eng, spin, size):
+    """Site dimensions 4 and 5 (S = 3/2 and 2, with a field; up to 57 vertices and 4 worm types
+    per bond type): the kernels' chains equal the oracle's."""
+    flat = S.flatten_model(S.MagnetModel({"lattice": {"unitcell": S.UnitCells.square, "size": size}, "S": spin,
+                                          "J": 1.0, "hz": 0.1, "measure": S.all_magnetization_estimators(2)}))
+    mid = eng.register_model(flat)
+    params = [dict(T=0.5, seed=61, stream=k, thermalization=5) for k in range(3)]
+    ids = eng.create_walkers(mid, params)
+    eng.init(ids)
+    eng.sweep(ids, 30, measure=True)
+    for p, wid in zip(params, ids.tolist()):
+        compare(eng, flat, wid, oracle_after(O, flat, p, 30))
