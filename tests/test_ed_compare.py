@@ -104,3 +104,24 @@ def test_oracle_vs_ed_higher_spin(S, O, spin, size, T):
         if z > 4:
             bad.append((name, mc, err, ref, z))
     assert not bad, bad
+
+
+def test_oracle_vs_ed_frustrated_triangle(S, O):
+    """The antiferromagnetic XXZ magnet on the triangular lattice (3x3, Jz = 1.4 J): negative vertex
+    weights (average sign about 0.22 at T = 1), so every observable is a ratio of signed means; the
+    oracle against exact diagonalisation, |z| <= 4."""
+    model = S.MagnetModel({"lattice": {"unitcell": S.UnitCells.triangle, "size": (3, 3)}, "J": 1.0, "d": 0.4,
+                           "measure": S.all_magnetization_estimators(2)})
+    flat = S.flatten_model(model)
+    assert (flat.arrays["sign"] < 0).any()
+    T = 1.0
+    ed = ed_observables(S, model, [T])
+    bins = run_binned(O, flat, T, seed=11, nbins=16, binsize=400, therm=1000)
+    bad = []
+    for name, f in evaluables(flat.est_prefixes, flat.norm_site_count).items():
+        mc, err = jackknife(bins, f)
+        ref = float(ed[name][0])
+        z = abs(mc - ref) / (err if err != 0 else 1e-8)
+        if z > 4:
+            bad.append((name, mc, err, ref, z))
+    assert not bad, bad

@@ -326,3 +326,20 @@ def test_emulated_higher_spin_matches_oracle(S, O, eng, spin, size):
     eng.sweep(ids, 30, measure=True)
     for p, wid in zip(params, ids.tolist()):
         compare(eng, flat, wid, oracle_after(O, flat, p, 30))
+
+
+@pytest.mark.parametrize("family", ["square_s1_field", "triangle_xxz"])
+def test_emulated_other_families_match_oracle(S, O, eng, family):
+    """The S=1 square lattice with a field and single-ion anisotropy, and the frustrated triangular
+    XXZ magnet (negative vertex weights, so signed measurements): the kernels' chains equal the
+    oracle's."""
+    from test_tables import families
+
+    flat = S.flatten_model(families(S)[family](S))
+    mid = eng.register_model(flat)
+    params = [dict(T=0.5, seed=71, stream=k, thermalization=4) for k in range(3)]
+    ids = eng.create_walkers(mid, params)
+    eng.init(ids)
+    eng.sweep(ids, 20, measure=True)
+    for p, wid in zip(params, ids.tolist()):
+        compare(eng, flat, wid, oracle_after(O, flat, p, 20))
