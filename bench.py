@@ -217,6 +217,47 @@ def cpu_baseline(S, flat, states, args, nthreads):
     }
 
 
+def parity_check(S, flat, eng, ids, states, args, nsweeps=5):
+    """The benchmarked walkers continued on both sides: `states` were exported after the timed
+    region; the same walkers run `nsweeps` more Carlo steps on the GPU and, imported, in the oracle.
+    Opstrings, spin states, cutoffs, replay counters and controller doubles must be equal bit for
+    bit, the observables of those sweeps within 1e-12 relative."""
+    from oracle import oracle as O
+
+    om = O.OracleModel(flat)
+    chains = []
+    for k, (ops, st, inf) in enumerate(states):
+        w = O.OracleWalker(om, T=1.0 / args.beta, seed=args.seed, stream=k, thermalization=args.therm)
+        w.set_opstring(ops, inf["num_operators"])
+        w.set_state(st)
+        w.w.ctr = inf["rng_counter"]
+        w.w.num_worms = inf["num_worms"]
+        w.w.avg_worm_length = inf["avg_worm_length"]
+        w.w.sweeps = inf["sweeps"]
+        chains.append(w)
+    sub = np.ascontiguousarray(ids[: len(states)], dtype=np.int32)
+    eng.observables(sub, reset=True)
+    eng.sweep(sub, nsweeps, measure=True)
+    O.run_parallel(om, chains, nsweeps, measure=True, nthreads=min(len(chains), os.cpu_count() or 1))
+    bad, worst = [], 0.0
+    for wid, w in zip(sub.tolist(), chains):
+        ops, st, inf = eng.export(wid)
+        same = (inf["status"] == w.w.status == 0 and inf["L"] == w.w.L and inf["rng_counter"] == w.w.ctr
+                and inf["num_operators"] == w.w.num_operators and inf["num_worms"] == w.w.num_worms
+                and inf["avg_worm_length"] == w.w.avg_worm_length and np.array_equal(ops, w.ops)
+                and np.array_equal(st, w.state))
+        s, c, _ = eng.observables([wid])[0]
+        so, co, _ = w.obs()
+        rel = float(np.max(np.abs(s - so) / np.maximum(np.abs(so), 1e-300))) if len(so) else 0.0
+        worst = max(worst, rel)
+        if not same or not np.array_equal(c, co) or rel > 1e-12:
+            bad.append(wid)
+    return {"walkers": len(chains), "sweeps": nsweeps, "bit_exact_walkers": len(chains) - len(bad),
+            "max_rel_observable_diff": worst, "mismatched_walkers": bad,
+            "what": "exported after the timed region, continued on the GPU and in the oracle; opstring, state, "
+                    "cutoff, replay counter and controller compared bit for bit, observables to 1e-12"}
+
+
 def run_serving(args, device):
     """The request loop: Poisson arrivals at 200 requests/s, continuous batching, p50/p99 time-to-result.
     The request distribution is the serving workload's, scaled so the run is bounded: side 8-24,
@@ -345,48 +386,89 @@ def run_other_workload(args):
     elif args.workload == "uneven":
         line.update(run_uneven_balanced(S, eng, args, rng))
     elif args.workload == "bilayer":
-        p = {"lattice": {"unitcell": S.UnitCells.square_bilayer, "size": (48, 48)}, "S": 1.0, "J": 1.0, "Jp": 0.5,
-             "parameter_map": {"J": ["Jp", "J", "J", "J", "J"]}, "Dz": 0.3, "hz": 0.2, "measure": ["magnetization"]}
-        mid = eng.register_model(S.flatten_model(S.MagnetModel(p)))
-        betas = [4.0, 8.0, 16.0]
-        # the walkers count the first --therm sweeps as thermalisation (Carlo's rule), so the timed
-        # steps run measure! and the worm-count controller is frozen, as in a production run
-        params = [(mid, dict(T=1.0 / betas[k % 3], seed=args.seed, stream=k, thermalization=args.therm))
-                  for k in range(2048)]
-        desc = "2048 walkers, S=1 square bilayer 48x48, J=1, J_perp=0.5, Dz=0.3, hz=0.2, beta in {4,8,16}"
-        ids = []
-        for m in sorted({m for m, _ in params}):
-            ids += eng.create_walkers(m, [q for mm, q in params if mm == m]).tolist()
-        ids = np.array(ids, dtype=np.int32)
-        eng.init(ids)
-        failed = 0
-        done = 0
-        t0 = time.perf_counter()
-        while done < args.therm:
-            ids, f = sweep_tolerant(eng, ids, min(25, args.therm - done), measure=False)
-            failed += f
-            done += min(25, args.therm - done)
-        therm_s = time.perf_counter() - t0
-        info0 = {i: eng.info(i) for i in ids.tolist()}
-        t_dev = 0.0
-        for _ in range(args.steps):
-            ids, f = sweep_tolerant(eng, ids, args.sweeps_per_step, measure=True)
-            failed += f
-            t_dev += eng.last_timing()[0] / 1e3
-        info1 = {i: eng.info(i) for i in ids.tolist()}
-        ws = len(ids) * args.sweeps_per_step * args.steps
-        ou = sum(info1[i]["slot_visits"] + info1[i]["worm_steps"] - info0[i]["slot_visits"] - info0[i]["worm_steps"]
-                 for i in ids.tolist())
-        Ls = np.array([info1[i]["L"] for i in ids.tolist()])
-        line.update(config=desc, thermalization_sweeps=args.therm, thermalization_seconds=therm_s,
-                    sweeps_per_step=args.sweeps_per_step, steps=args.steps, walker_sweeps_per_s=ws / t_dev,
-                    operator_updates_per_s=ou / t_dev, walkers_stopped_by_worm_cap=failed,
-                    thermalisation_sweeps_undone_at_worm_cap=sum(info1[i]["worm_undos"] for i in ids.tolist()),
-                    cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
+        line.update(run_bilayer(S, eng, args))
     elif args.workload in ("magnet_bench", "cluster_bench"):
         line.update(run_reference_job(S, eng, args))
     eng.close()
     print(json.dumps(line), flush=True)
+
+
+def balanced_counts(cost, kmax=4096):
+    """Per-walker sweep counts for one cost-balanced block: walker i runs round(c_max / c_i) sweeps,
+    c_i its device clock cycles per sweep in the last block, so that every walker works about as
+    long as one sweep of the slowest."""
+    cost = np.maximum(np.asarray(cost, dtype=np.float64), 1.0)
+    return np.clip(np.rint(cost.max() / cost), 1, kmax).astype(np.int32)
+
+
+def run_bilayer(S, eng, args):
+    """The larger-local-space workload: S=1 Heisenberg antiferromagnet on a 48x48 periodic square
+    bilayer (4608 sites, 11520 bonds), J=1, J_perp=0.5, Dz=0.3, hz=0.2, tables from the LP vertex
+    builder; 2048 walkers, a third each at beta = 4, 8 and 16, in one batch.
+
+    Opstring capacity is reserved up front at 1.25 x 13.2 N beta slots (the cutoff the reference's
+    growth rule reaches; 13.2 N beta measured on the 12x12 bilayer), so that walkers do not stop for
+    regrowth relaunches.  Thermalisation (`--therm` sweeps per walker, worm-count controller active)
+    runs in cost-balanced sse_sweep_each blocks: every walker gets round(c_max / c_i) sweeps, capped
+    at what it still needs, so a slow walker or a long early worm does not leave the batch idle for
+    many sweeps.  Then `--steps` balanced blocks with measure! are timed."""
+    p = {"lattice": {"unitcell": S.UnitCells.square_bilayer, "size": (48, 48)}, "S": 1.0, "J": 1.0, "Jp": 0.5,
+         "parameter_map": {"J": ["Jp", "J", "J", "J", "J"]}, "Dz": 0.3, "hz": 0.2, "measure": ["magnetization"]}
+    flat = S.flatten_model(S.MagnetModel(p))
+    mid = eng.register_model(flat)
+    betas = np.array([4.0, 8.0, 16.0])
+    nw = 2048
+    beta_of = betas[np.arange(nw) % 3]
+    params = [dict(T=1.0 / float(beta_of[k]), seed=args.seed, stream=k, thermalization=args.therm) for k in range(nw)]
+    ids = eng.create_walkers(mid, params)
+    t0 = time.perf_counter()
+    for b in betas:
+        eng.reserve(ids[beta_of == b], int(1.25 * 13.2 * flat.nsites * b))
+    eng.init(ids)
+
+    def counters():
+        inf = [eng.info(int(i)) for i in ids]
+        return (np.array([x["sweeps"] for x in inf], dtype=np.int64),
+                np.array([sum(x["phase_cycles"]) for x in inf], dtype=np.float64),
+                np.array([x["slot_visits"] + x["worm_steps"] for x in inf], dtype=np.float64), inf)
+
+    sw, cy, ou, _ = counters()
+    k = np.ones(nw, dtype=np.int32)
+    blocks = 0
+    therm_dev = 0.0
+    while sw.min() < args.therm:
+        k = np.minimum(k, np.maximum(args.therm - sw, 0)).astype(np.int32)
+        eng.sweep_each(ids, k, measure=True)
+        therm_dev += eng.last_timing()[0] / 1e3
+        sw1, cy1, ou1, _ = counters()
+        k = balanced_counts((cy1 - cy) / np.maximum(sw1 - sw, 1))
+        sw, cy, ou = sw1, cy1, ou1
+        blocks += 1
+    therm_s = time.perf_counter() - t0
+    dev = 0.0
+    sw_start, ou_start = sw.copy(), ou.copy()
+    per_beta_dev = []
+    for _ in range(args.steps):
+        eng.sweep_each(ids, k, measure=True)
+        dev += eng.last_timing()[0] / 1e3
+        sw1, cy1, ou1, inf = counters()
+        k = balanced_counts((cy1 - cy) / np.maximum(sw1 - sw, 1))
+        sw, cy, ou = sw1, cy1, ou1
+    Ls = np.array([x["L"] for x in inf])
+    dsw, dou = sw - sw_start, ou - ou_start
+    return dict(
+        config="2048 walkers, S=1 square bilayer 48x48 (4608 sites), J=1, J_perp=0.5, Dz=0.3, hz=0.2, "
+               "beta in {4,8,16} (a third each); cost-balanced sse_sweep_each blocks",
+        thermalization_sweeps=args.therm, thermalization_blocks=blocks, thermalization_seconds_wall=therm_s,
+        thermalization_seconds_device=therm_dev, steps=args.steps,
+        walker_sweeps_per_s=float(dsw.sum()) / dev, operator_updates_per_s=float(dou.sum()) / dev,
+        per_beta={str(b): {"walker_sweeps_per_s": float(dsw[beta_of == b].sum()) / dev,
+                           "operator_updates_per_walker_sweep": float(dou[beta_of == b].sum() / max(dsw[beta_of == b].sum(), 1)),
+                           "cutoff_L_median": int(np.median(Ls[beta_of == b]))} for b in betas.tolist()},
+        sweeps_per_block_min_median_max=[int(k.min()), int(np.median(k)), int(k.max())],
+        walkers_stopped=int(sum(x["status"] != 0 for x in inf)),
+        thermalisation_sweeps_undone_at_worm_cap=int(sum(x["worm_undos"] for x in inf)),
+        cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
 
 
 def run_uneven_balanced(S, eng, args, rng):
@@ -566,9 +648,9 @@ def main():
         blk = min(100, args.therm - done)
         eng.sweep(ids, blk, measure=True)
         done += blk
-    launches_seen = 0
+    # the sweep blocks run as CUDA-graph replays (the first warm-up step captures the block)
     for _ in range(args.warmup):
-        eng.sweep(ids, args.sweeps_per_step, measure=True)
+        eng.sweep(ids, args.sweeps_per_step, measure=True, graph=True)
         eng.observables(ids, reset=True)
 
     info0 = [eng.info(int(i)) for i in ids]
@@ -580,7 +662,7 @@ def main():
     if args.profile:
         eng.profiler_range(True)
     for _ in range(args.steps):
-        eng.sweep(ids, args.sweeps_per_step, measure=True)
+        eng.sweep(ids, args.sweeps_per_step, measure=True, graph=True)
         ms, nl = eng.last_timing()
         step_ms.append(ms)
         launches += nl
@@ -620,14 +702,24 @@ def main():
     t0 = time.perf_counter()
     obs_bytes = 0
     for _ in range(args.steps):
-        eng.sweep(ids, args.sweeps_per_step, measure=True)
+        eng.sweep(ids, args.sweeps_per_step, measure=True, graph=True)
         out = eng.observables(ids, reset=True)
         obs_bytes = sum(s.nbytes + c.nbytes + l.nbytes for s, c, l in out)
     e2e_s = barrier_max(world, time.perf_counter() - t0)
     e2e_value = total_ws / e2e_s
 
+    # the same sweep block launched directly instead of from the captured graph
+    direct_ms = []
+    for _ in range(min(2, args.steps)):
+        eng.sweep(ids, args.sweeps_per_step, measure=True)
+        direct_ms.append(eng.last_timing()[0])
+    direct_value = nw * args.sweeps_per_step / (np.mean(direct_ms) / 1e3) if direct_ms else None
+
     result = None
     if rank == 0:
+        nchk = min(16, nw, args.cpu_threads or os.cpu_count() or 1)
+        states = [eng.export(int(i)) for i in ids[: max(nchk, args.cpu_threads or os.cpu_count() or 1)]]
+        parity = parity_check(S, flat, eng, ids, states[:nchk], args)
         # plain path: one launch per walker per sweep (a per-walker sweep! call)
         sub = ids[: args.plain_walkers]
         eng.sweep(sub, 1, measure=True, plain=True)
@@ -636,7 +728,6 @@ def main():
         plain_s = time.perf_counter() - t0
         plain_value = len(sub) * 2 / plain_s
 
-        states = [eng.export(int(i)) for i in ids[: (args.cpu_threads or os.cpu_count() or 1)]]
         cpu = cpu_baseline(S, flat, states, args, args.cpu_threads or os.cpu_count() or 1)
         serving = run_serving(args, local) if args.serving_requests > 0 else None
 
@@ -693,11 +784,17 @@ def main():
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": 4 * len(ids),
                     "d2h_bytes_per_step": obs_bytes},
             "gpu_launches": launches,
+            "launch_path": "CUDA-graph replay of the sweep block (flag/queue resets + one persistent launch)",
+            "direct_launch_value": direct_value,
+            "parity_checked": not parity["mismatched_walkers"],
+            "parity": parity,
             "clocks": clk,
             "serving": serving,
         }
         print(json.dumps(result), flush=True)
     eng.close()
+    if result is not None and not result["parity_checked"]:
+        sys.exit("bench: the benchmarked walkers left the oracle's chain: " + str(result["parity"]))
     if world > 1:
         import torch.distributed as dist
 

@@ -275,7 +275,23 @@ int sse_sweep_tempering(sse_engine *eng, int32_t nladders, int32_t nrungs, const
  * last call's contents in it; everything a call reads from it is rewritten
  * by that call first.  Calls whose device work overlaps (several host
  * threads, several streams) race on the array and must be serialised by the
- * caller.  The call is synchronous and returns the walker's sse_status. */
+ * caller.  The call is synchronous and returns the walker's sse_status.
+ *
+ * Streams: the call launches its kernels on the legacy default stream and
+ * waits for them before it returns.  The legacy default stream is ordered
+ * after work on ordinary (blocking) streams, but not after work on streams
+ * created with cudaStreamNonBlocking -- PyTorch's side streams, CUDA.jl's
+ * per-task streams and most library streams are of that kind.  A caller
+ * whose buffers (model tables, walker, opstring, state, observables) were
+ * written on such a stream must synchronise that stream before the call.
+ *
+ * Input checks: before it sweeps, the call checks on the device what the
+ * engine's sse_model_register and sse_walker_import check on the host --
+ * bond sites and types, type sizes and table offsets, leg states, the
+ * diagonal-vertex table, every transition row and scatter outcome, and for a
+ * walker past Carlo.init! its cutoff, opstring and spin state -- and returns
+ * SSE_ERR_ARG (SSE_ERR_UNSUPPORTED for a transition row longer than 256
+ * outcomes) without touching the walker's chain when one fails. */
 #define SSE_NOALLOC_MAX_SLOTS (1 << 18)    /* opstring capacity (cutoff L) */
 #define SSE_NOALLOC_MAX_SITES (1 << 14)
 #define SSE_NOALLOC_MAX_BONDS (1 << 16)
@@ -293,7 +309,9 @@ typedef struct sse_noalloc_walker {
   uint64_t stream;
   int64_t init_opstring_cutoff;
   int32_t diagonal_warmup_sweeps;
-  int32_t phase;       /* 0: Carlo.init! still to run (set by the caller), 2: initialised */
+  int32_t phase;       /* 0: Carlo.init! still to run (set by the caller), 1: its diagonal warm-up
+                          sweeps under way (left by a call stopped for capacity), 2: initialised;
+                          any other value is refused with SSE_ERR_ARG */
   double init_num_worms;
   double num_worms_attenuation_factor;
   double target_worm_length_fraction;

@@ -646,64 +646,62 @@ struct WormCtl {
   double num_worms, avg_len, att, target_frac;
 };
 
-__device__ __forceinline__ void prefetch_l1(const void *p) {
-  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
-}
-
-// State of a worm between draw-buffer refills (lane 0's registers).
+// Lane 0's chase of one worm between draw-buffer refills.
 struct Chase {
   int k, leg_in, wf;
   long long len;
   int4 ra, rb;  // record of operator k: links, then (op, slot, transition offset, type info)
 };
 
-// Steps of one worm run by lane 0 while draws remain in the buffer (src/sse.jl:262-303
-// with scatter, src/vertex_data.jl:106-125).  Per step: one 32-byte record from DRAM and
-// one transition row from L1; when a record arrives its four neighbours are prefetched
-// into L1 so that the next record is in flight while the scatter resolves.  Returns with
-// `done` set when the worm closes, or with pos == DRAW_BUF when the buffer is empty.
+// What one call of worm_chase needs besides the tables: the draw position in the 64-draw buffer
+// (in and out), the worm's start (k0, l0, wf0) and the steps left before the cap.
+struct ChaseWindow {
+  int pos, k0, l0, wf0, room, done;
+};
+
+// Steps of one worm run by lane 0 while draws remain in the buffer (src/sse.jl:262-303 with
+// scatter, src/vertex_data.jl:106-125).  Per step: one 32-byte record (its links, code and type
+// info) and the first 16 bytes of one transition row from L1 (threshold and packed outcome of the
+// row's first outcome; the second half only when the first outcome is not taken).  Kept out of
+// line, with its state in a handful of registers, so that the loop does not share the register
+// budget of the worm update's other phases.
 //
-// PF false: the records are staged in shared memory and nothing is prefetched.
-template <bool PF>
-__device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long long *dbuf, int &pos,
-                                          uint32_t *__restrict__ ops, Rec *__restrict__ rec, int k0, int l0, int wf0,
-                                          long long cap, Chase &cs, bool &done) {
-  const Trans *__restrict__ trans = M.trans;
-  const Outcome *__restrict__ outc = M.outc;
+// The records of the worm's possible next operators are not prefetched: at 4096 walkers the three
+// extra random sector reads per step cost the diagonal and link phases more than the ~110 cycles
+// they save the step (A/B on the 32x32, beta = 16 batch: 75.9k vs 75.4k walker-sweeps/s).
+// Returns the status; sets win.done when the worm closed; win.pos == 64 when the buffer ran dry.
+__device__ __noinline__ int worm_chase(const Trans *__restrict__ trans, const Outcome *__restrict__ outc,
+                                       Rec *__restrict__ rec, const unsigned long long *__restrict__ dbuf,
+                                       Chase *cs, ChaseWindow *win) {
+  int k = cs->k, leg_in = cs->leg_in, wf = cs->wf;
+  int4 ra = cs->ra;
+  uint32_t op = (uint32_t)cs->rb.x;
+  int slot = cs->rb.y, toff = cs->rb.z, tp = cs->rb.w;
+  int pos = win->pos;
+  const int k0 = win->k0, l0 = win->l0, wf0 = win->wf0, room = win->room;
   const int4 *rq = reinterpret_cast<const int4 *>(rec);
-  int k = cs.k, leg_in = cs.leg_in, wf = cs.wf;
-  const long long len0 = cs.len;
-  // steps left before the worm exceeds the cap (a draw window has at most 64 steps)
-  const int room = (cap - len0) > 0x3FFFFFFFLL ? 0x3FFFFFFF : (int)(cap - len0);
-  int used = 0;
-  int4 ra = cs.ra, rb = cs.rb;
-  int status = ST_OK;
+  uint32_t *rop = reinterpret_cast<uint32_t *>(rec);  // rec[k].op = rop[8 k + 4]
+  int used = 0, status = ST_OK, done = 0;
   while (pos < 64) {
     const unsigned long long u53 = dbuf[pos];
     pos++;
-    if (PF) {
-      prefetch_l1(rq + 2 * (ra.x >> 2));
-      prefetch_l1(rq + 2 * (ra.y >> 2));
-      prefetch_l1(rq + 2 * (ra.z >> 2));
-      prefetch_l1(rq + 2 * (ra.w >> 2));
-    }
-    const uint32_t op = (uint32_t)rb.x;
-    const int vc = (int)((op >> 1) & 0x3FFu);
-    const int ti = rb.z + ((vc >> 1) * 4 + leg_in) * (rb.w & 0xFF) + (wf - 1);
-    const Trans tr = trans[ti];
-    int packed = tr.packed0;
-    if (packed >= 0 && !(u53 < tr.thr0)) {
-      packed = tr.packed1;
-      if (packed >= 0 && !(u53 < tr.thr1)) {
-      packed = -1;
-      const int o0 = tr.rest >> 8, on = tr.rest & 0xFF;
-      for (int o = o0; o < o0 + on; o++) {
-        const Outcome oc = outc[o];
-        if (u53 < oc.thr) {
-          packed = oc.packed;
-          break;
+    const int ti = toff + ((int)((op >> 2) & 0x1FFu) * 4 + leg_in) * (tp & 0xFF) + (wf - 1);
+    const int4 *tr = reinterpret_cast<const int4 *>(trans + ti);
+    const int4 h0 = __ldg(tr);  // thr0, packed0, rest
+    int packed = h0.z;
+    if (packed >= 0 && !(u53 < (((unsigned long long)(uint32_t)h0.y << 32) | (uint32_t)h0.x))) {
+      const int4 h1 = __ldg(tr + 1);  // thr1, packed1
+      packed = h1.z;
+      if (packed >= 0 && !(u53 < (((unsigned long long)(uint32_t)h1.y << 32) | (uint32_t)h1.x))) {
+        packed = -1;
+        const int o0 = h0.w >> 8, on = h0.w & 0xFF;
+        for (int o = o0; o < o0 + on; o++) {
+          const Outcome oc = outc[o];
+          if (u53 < oc.thr) {
+            packed = oc.packed;
+            break;
+          }
         }
-      }
       }
     }
     if (packed < 0) {
@@ -712,25 +710,21 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
     }
     const int leg_out = packed & 3;
     const int wf_out = (packed >> 2) & 0xFF;
-    const uint32_t nop = 1u | ((uint32_t)((packed >> 10) & 0x3FF) << 1) | (op & 0xFFFFF800u);
-    const int slot = rb.y;
-    const int kcur = k;
     const int dim_out = (packed >> 20) & 0xFF;
-    bool fin = (k == k0 && leg_out == l0 && wf_out == dim_out - wf0);
-    if (!fin) {
-      used += 1;
-      wf = wf_out;
-      const int link = leg_out == 0 ? ra.x : leg_out == 1 ? ra.y : leg_out == 2 ? ra.z : ra.w;
-      leg_in = link & 3;
-      k = link >> 2;
-      fin = (k == k0 && leg_in == l0 && wf == wf0);
-    }
     // the store precedes the next load of the same record, so a revisit sees the new code; the
     // opstring itself is written once after the worms (slot order, coalesced)
-    rec[kcur].op = nop;
-    (void)slot;
-    if (fin) {
-      done = true;
+    rop[8 * k + 4] = 1u | ((uint32_t)((packed >> 10) & 0x3FF) << 1) | (op & 0xFFFFF800u);
+    if (k == k0 && leg_out == l0 && wf_out == dim_out - wf0) {
+      done = 1;
+      break;
+    }
+    used++;
+    wf = wf_out;
+    const int link = leg_out == 0 ? ra.x : leg_out == 1 ? ra.y : leg_out == 2 ? ra.z : ra.w;
+    leg_in = link & 3;
+    k = link >> 2;
+    if (k == k0 && leg_in == l0 && wf == wf0) {
+      done = 1;
       break;
     }
     if (used > room) {  // len0 + used > cap
@@ -738,14 +732,20 @@ __device__ __forceinline__ int worm_steps(const DevModel &M, const unsigned long
       break;
     }
     ra = rq[2 * k];
-    rb = rq[2 * k + 1];
+    const int4 rb = rq[2 * k + 1];
+    op = (uint32_t)rb.x;
+    slot = rb.y;
+    toff = rb.z;
+    tp = rb.w;
   }
-  cs.k = k;
-  cs.leg_in = leg_in;
-  cs.wf = wf;
-  cs.len = len0 + used;
-  cs.ra = ra;
-  cs.rb = rb;
+  cs->k = k;
+  cs->leg_in = leg_in;
+  cs->wf = wf;
+  cs->len += used;
+  cs->ra = ra;
+  cs->rb = make_int4((int)op, slot, toff, tp);
+  win->pos = pos;
+  win->done = done;
   return status;
 }
 
@@ -753,7 +753,7 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
                                         Rec *__restrict__ rec, const int32_t *__restrict__ cidx,
                                         const int32_t *__restrict__ vfirst, uint8_t *__restrict__ state,
                                         unsigned long long *dbuf, bool thermalized, double &wlf, bool &have_wlf,
-                                        long long &steps, int lane, bool pf, int cap_factor) {
+                                        long long &steps, int lane, int cap_factor) {
   double total = 1.0;
   const double ceil_nw = ceil(wc.num_worms);
   const long long nworms = (long long)ceil_nw;
@@ -811,8 +811,17 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
       __syncwarp();
       int pos = (int)(ctr - b);
       if (lane == 0) {
-        if (pf) status = worm_steps<true>(M, dbuf, pos, ops, rec, k0, l0, wf0, cap, cs, done);
-        else status = worm_steps<false>(M, dbuf, pos, ops, rec, k0, l0, wf0, cap, cs, done);
+        // steps left before the worm exceeds the cap (a draw window has at most 64 steps)
+        ChaseWindow win;
+        win.pos = pos;
+        win.k0 = k0;
+        win.l0 = l0;
+        win.wf0 = wf0;
+        win.room = (cap - cs.len) > 0x3FFFFFFFLL ? 0x3FFFFFFF : (int)(cap - cs.len);
+        win.done = 0;
+        status = worm_chase(M.trans, M.outc, rec, dbuf, &cs, &win);
+        pos = win.pos;
+        done = win.done != 0;
       }
       __syncwarp();
       status = __shfl_sync(FULL, status, 0);

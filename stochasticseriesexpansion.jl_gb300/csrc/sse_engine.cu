@@ -127,7 +127,7 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
         bool have_wlf = false;
         status = worm_update(M, c, wc, ops, wrec, W->cidx, W->vfirst, state,
                              reinterpret_cast<unsigned long long *>(smem), thermalized, wlf, have_wlf, worm_steps,
-                             lane, !staged, W->cap_factor);
+                             lane, W->cap_factor);
         if (status == ST_WORM_UNDONE) {  // rare: counted straight in the walker record
           status = ST_OK;
           if (lane == 0) W->worm_undos++;
@@ -1031,7 +1031,10 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
     x.trans_off = d->type_trans_off[t];
     x.pad = 0;
     if (x.nverts <= 0 || x.nverts > 512) return fail(e, SSE_ERR_UNSUPPORTED, "vertex count per type must be 1..512");
-    if (x.d0 < 2 || x.d1 < 2 || x.maxworm < 1) return fail(e, SSE_ERR_ARG, "bad type dims");
+    // maxworm and the dimensions share one packed word in the compact records (8 bits each)
+    if (x.d0 < 2 || x.d1 < 2 || x.d0 > 255 || x.d1 > 255 || x.maxworm < 1 || x.maxworm > 255)
+      return fail(e, SSE_ERR_ARG, "bad type dims");
+    if (x.diag_off < 0 || x.vert_off < 0 || x.trans_off < 0) return fail(e, SSE_ERR_ARG, "negative table offset");
     ndiag = std::max(ndiag, (size_t)x.diag_off + (size_t)x.d0 * x.d1);
     nvert = std::max(nvert, (size_t)x.vert_off + x.nverts);
     ntrans = std::max(ntrans, (size_t)x.trans_off + (size_t)x.nverts * 4 * x.maxworm);
@@ -1039,6 +1042,9 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
   for (size_t i = 0; i < ntrans; i++) {
     if (d->trans_start[i] >= 0) nout = std::max(nout, (size_t)d->trans_start[i] + (size_t)d->trans_count[i]);
   }
+  for (int i = 0; i < d->nsites; i++)
+    if (d->site_dims[i] < 1 || d->site_dims[i] > d->maxdim)
+      return fail(e, SSE_ERR_ARG, "site " + std::to_string(i) + " has a dimension outside 1..maxdim");
   for (int b = 0; b < d->nbonds; b++) {
     const DevType &x = types[bi[b].z];
     if (d->site_dims[bi[b].x] != x.d0 || d->site_dims[bi[b].y] != x.d1)
@@ -1058,7 +1064,9 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
   if (!rc) rc = upload(e, hm, types.data(), types.size(), &m.types);
   if (!rc) rc = upload(e, hm, d->diag_vertex, ndiag, &m.diag_vertex);
   // weight classes: the distinct weights of diagonal vertices; the diagonal update compares
-  // random integers against per-class thresholds
+  // random integers against per-class thresholds.  With more than 32 classes it compares against
+  // each vertex's own weight instead and uses the class (clamped to 127) only to tell a diagonal
+  // vertex from an off-diagonal one, so any number of distinct weights is handled exactly.
   std::vector<double> cls_w;
   std::vector<int8_t> vclass(nvert, (int8_t)-1);
   for (int t = 0; t < d->ntypes; t++) {
@@ -1114,7 +1122,11 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
   for (int t = 0; t < d->ntypes; t++) {
     const size_t r0 = (size_t)d->type_trans_off[t];
     const size_t r1 = r0 + (size_t)types[t].nverts * 4 * types[t].maxworm;
-    for (size_t r = r0; r < r1 && r < ntrans; r++) row_type[r] = t;
+    for (size_t r = r0; r < r1 && r < ntrans; r++) {
+      // a row shared by two types would be checked against one type's tables and walked by the other's
+      if (row_type[r] >= 0) return fail(e, SSE_ERR_ARG, "two bond types share transition rows");
+      row_type[r] = t;
+    }
   }
   std::vector<Trans> trans(ntrans);
   for (size_t i = 0; i < ntrans; i++) {
@@ -1833,6 +1845,7 @@ struct NoAllocScratch {
   DevType types[SSE_NOALLOC_MAX_TYPES];
   int32_t diag_vc[SSE_NOALLOC_MAX_DIAG];
   int8_t vclass[SSE_NOALLOC_MAX_VERTICES];
+  int32_t row_owner[SSE_NOALLOC_MAX_TRANSITIONS];
   double cls_w[128];
   DevModel model;
   DevWalker walker;
@@ -1843,69 +1856,97 @@ struct NoAllocScratch {
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
 // Derives the engine's model tables from the caller's flat tables (device pointers) and
-// loads the caller's walker into the scratch.  One block; writes status != 0 on overflow.
+// loads the caller's walker into the scratch.  One block.  Before anything is derived it checks
+// what sse_model_register and sse_walker_import check on the host, so that no later kernel
+// indexes outside a table; on failure it writes the status to X->status and to the walker and
+// leaves the walker's chain as it was.
 __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_walker *uw, uint32_t *ops,
                                long long ops_capacity, uint8_t *state, double *obs_sum, long long *obs_count,
                                double *obs_last) {
-  __shared__ int s_sizes[4];  // ndiag, nvert, ntrans, nout
+  __shared__ int s_sizes[4];  // ndiag, nvert, ntrans, nout (each at most its limit + 1)
   __shared__ int s_ncls;
+  __shared__ int s_bad, s_unsup;
   const int tid = threadIdx.x, nt = blockDim.x;
+  const auto clip = [](long long x, int lim) { return (int)(x > lim ? lim + 1 : x); };
   if (tid == 0) {
     X->status = SSE_OK;
-    int ndiag = 0, nvert = 0, ntrans = 0;
+    s_bad = 0;
+    s_unsup = 0;
+    long long ndiag = 0, nvert = 0, ntrans = 0;
     for (int t = 0; t < d.ntypes; t++) {
       const int d0 = d.type_dims[2 * t], d1 = d.type_dims[2 * t + 1];
-      ndiag = max(ndiag, d.type_diag_off[t] + d0 * d1);
-      nvert = max(nvert, d.type_vert_off[t] + d.type_nverts[t]);
-      ntrans = max(ntrans, d.type_trans_off[t] + d.type_nverts[t] * 4 * d.type_maxworm[t]);
-      if (d0 < 2 || d1 < 2 || d0 > 255 || d1 > 255 || d.type_maxworm[t] < 1 || d.type_nverts[t] < 1 ||
-          d.type_nverts[t] > 512)
+      const int nv = d.type_nverts[t], mw = d.type_maxworm[t];
+      const int doff = d.type_diag_off[t], voff = d.type_vert_off[t], toff = d.type_trans_off[t];
+      // maxworm and the dimensions share one packed word in the compact records (8 bits each)
+      if (d0 < 2 || d1 < 2 || d0 > 255 || d1 > 255 || mw < 1 || mw > 255 || nv < 1 || nv > 512 || doff < 0 ||
+          voff < 0 || toff < 0) {
         X->status = SSE_ERR_ARG;
-    }
-    s_sizes[0] = ndiag;
-    s_sizes[1] = nvert;
-    s_sizes[2] = ntrans;
-    s_sizes[3] = 0;
-  }
-  __syncthreads();
-  for (int i = tid; i < s_sizes[2]; i += nt) {
-    const int st = d.trans_start[i];
-    if (st >= 0) atomicMax(&s_sizes[3], st + d.trans_count[i]);
-  }
-  __syncthreads();
-  if (tid == 0) {
-    if (s_sizes[0] > SSE_NOALLOC_MAX_DIAG || s_sizes[1] > SSE_NOALLOC_MAX_VERTICES ||
-        s_sizes[2] > SSE_NOALLOC_MAX_TRANSITIONS || s_sizes[3] > SSE_NOALLOC_MAX_OUTCOMES)
-      X->status = SSE_ERR_CAPACITY;
-    // weight classes of the diagonal vertices, in vertex order (as sse_model_register)
-    int ncls = 0;
-    for (int v = 0; v < s_sizes[1] && v < SSE_NOALLOC_MAX_VERTICES; v++) X->vclass[v] = -1;
-    if (X->status == SSE_OK) {
-      for (int t = 0; t < d.ntypes; t++) {
-        for (int v = 0; v < d.type_nverts[t]; v++) {
-          const int vo = d.type_vert_off[t] + v;
-          const uint8_t *ls = d.leg_state + 4 * vo;
-          if (ls[0] != ls[2] || ls[1] != ls[3]) continue;
-          const double w = d.weight[vo];
-          int c = 0;
-          while (c < ncls && X->cls_w[c] != w) c++;
-          if (c == ncls && ncls < 128) X->cls_w[ncls++] = w;
-          X->vclass[vo] = (int8_t)min(c, 127);
-        }
+        continue;
       }
+      ndiag = max(ndiag, (long long)doff + d0 * d1);
+      nvert = max(nvert, (long long)voff + nv);
+      ntrans = max(ntrans, (long long)toff + (long long)nv * 4 * mw);
     }
-    s_ncls = ncls;
+    s_sizes[0] = clip(ndiag, SSE_NOALLOC_MAX_DIAG);
+    s_sizes[1] = clip(nvert, SSE_NOALLOC_MAX_VERTICES);
+    s_sizes[2] = clip(ntrans, SSE_NOALLOC_MAX_TRANSITIONS);
+    s_sizes[3] = 0;
+    if (X->status == SSE_OK && (ndiag > SSE_NOALLOC_MAX_DIAG || nvert > SSE_NOALLOC_MAX_VERTICES ||
+                                ntrans > SSE_NOALLOC_MAX_TRANSITIONS))
+      X->status = SSE_ERR_CAPACITY;
+  }
+  __syncthreads();
+  if (X->status == SSE_OK) {
+    // the outcome table's size: every row that has outcomes ends inside it
+    for (int i = tid; i < s_sizes[2]; i += nt) {
+      const int st = d.trans_start[i], cnt = d.trans_count[i];
+      if (st >= 0 && cnt > 0) atomicMax(&s_sizes[3], clip((long long)st + cnt, SSE_NOALLOC_MAX_OUTCOMES));
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && X->status == SSE_OK) {
+    if (s_sizes[3] > SSE_NOALLOC_MAX_OUTCOMES) X->status = SSE_ERR_CAPACITY;
   }
   __syncthreads();
   if (X->status != SSE_OK) {
     if (tid == 0) uw->status = X->status;
     return;
   }
-  // the contents the sweep indexes with: bonds, leg states, scatter outcomes and, for a walker that
-  // continues, its opstring and spin state (as sse_model_register and sse_walker_import check them)
-  __shared__ int s_bad;
-  if (tid == 0) s_bad = 0;
+  // which bond type owns each transition row (-1: none); a row claimed by two types is refused
+  for (int i = tid; i < s_sizes[2]; i += nt) X->row_owner[i] = -1;
   __syncthreads();
+  for (int t = 0; t < d.ntypes; t++) {
+    const int r0 = d.type_trans_off[t], r1 = r0 + d.type_nverts[t] * 4 * d.type_maxworm[t];
+    for (int i = r0 + tid; i < r1; i += nt)
+      if (atomicCAS(&X->row_owner[i], -1, t) != -1) s_bad = 1;
+  }
+  // weight classes of the diagonal vertices, in vertex order (as sse_model_register): with more
+  // than 32 classes the diagonal update compares against each vertex's own weight and uses the
+  // class (clamped to 127) only to tell a diagonal vertex from an off-diagonal one
+  for (int v = tid; v < s_sizes[1]; v += nt) X->vclass[v] = -1;
+  __syncthreads();
+  if (tid == 0) {
+    int ncls = 0;
+    for (int t = 0; t < d.ntypes; t++) {
+      for (int v = 0; v < d.type_nverts[t]; v++) {
+        const int vo = d.type_vert_off[t] + v;
+        const uint8_t *ls = d.leg_state + 4 * vo;
+        if (ls[0] != ls[2] || ls[1] != ls[3]) continue;
+        const double w = d.weight[vo];
+        int c = 0;
+        while (c < ncls && c < 128 && X->cls_w[c] != w) c++;
+        if (c == ncls) {
+          if (ncls < 128) X->cls_w[ncls] = w;
+          ncls++;
+        }
+        X->vclass[vo] = (int8_t)min(c, 127);
+      }
+    }
+    s_ncls = ncls;
+  }
+  __syncthreads();
+  // the contents the sweep indexes with: bonds, leg states, the diagonal-vertex table, scatter rows
+  // and outcomes and, for a walker past its first call, its opstring and spin state
   for (int b = tid; b < d.nbonds; b += nt) {
     const int s0 = d.bond_sites[2 * b], s1 = d.bond_sites[2 * b + 1], t = d.bond_type[b];
     if (s0 < 0 || s1 < 0 || s0 >= d.nsites || s1 >= d.nsites || s0 == s1 || t < 0 || t >= d.ntypes)
@@ -1913,43 +1954,63 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
     else if (d.site_dims[s0] != d.type_dims[2 * t] || d.site_dims[s1] != d.type_dims[2 * t + 1])
       s_bad = 1;
   }
-  for (int t = 0; t < d.ntypes; t++)
-    for (int x = tid; x < 4 * d.type_nverts[t]; x += nt)
-      if (d.leg_state[4 * d.type_vert_off[t] + x] >= d.type_dims[2 * t + (x & 1)]) s_bad = 1;
+  for (int i = tid; i < d.nsites; i += nt)
+    if (d.site_dims[i] < 1 || d.site_dims[i] > d.maxdim) s_bad = 1;
   for (int t = 0; t < d.ntypes; t++) {
-    const int r0 = d.type_trans_off[t], r1 = r0 + d.type_nverts[t] * 4 * d.type_maxworm[t];
+    const int d0 = d.type_dims[2 * t], d1 = d.type_dims[2 * t + 1], nv = d.type_nverts[t];
+    for (int x = tid; x < 4 * nv; x += nt)
+      if (d.leg_state[4 * d.type_vert_off[t] + x] >= ((x & 1) ? d1 : d0)) s_bad = 1;
+    for (int st = tid; st < d0 * d1; st += nt) {
+      const int vc = d.diag_vertex[d.type_diag_off[t] + st];
+      if (vc < 0) continue;
+      if (!(vc & 1) || (vc >> 1) >= nv || X->vclass[d.type_vert_off[t] + (vc >> 1)] < 0) s_bad = 1;
+    }
+    const int r0 = d.type_trans_off[t], r1 = r0 + nv * 4 * d.type_maxworm[t];
     for (int i = r0 + tid; i < r1; i += nt) {
-      const int st = d.trans_start[i];
-      if (st < 0) continue;
-      for (int o = st; o < st + d.trans_count[i]; o++)
+      const int st = d.trans_start[i], cnt = d.trans_count[i];
+      if (st < 0 || cnt <= 0) continue;
+      if (cnt > 256 || st + 2 >= (1 << 23)) {
+        s_unsup = 1;
+        continue;
+      }
+      for (int o = st; o < st + cnt; o++)
         if (d.out_leg[o] < 0 || d.out_leg[o] > 3 || d.out_worm[o] < 1 || d.out_worm[o] > d.type_maxworm[t] ||
-            d.out_target[o] < 0 || (d.out_target[o] >> 1) >= d.type_nverts[t])
+            d.out_target[o] < 0 || (d.out_target[o] >> 1) >= nv)
           s_bad = 1;
     }
   }
+  // rows with outcomes outside every type's range: the host refuses them too
+  for (int i = tid; i < s_sizes[2]; i += nt)
+    if (X->row_owner[i] < 0 && d.trans_start[i] >= 0 && d.trans_count[i] > 0) s_bad = 1;
   __syncthreads();
   // the walker's own state, read only once the tables it indexes are known to be valid
-  if (!s_bad && uw->phase == PH_READY) {
-    const long long L = uw->L, n = uw->num_operators;
-    if (L < 0 || L > ops_capacity || n < 0 || n > L) {
+  const int phase = uw->phase;
+  if (!s_bad && !s_unsup) {
+    if ((phase != PH_NEW && phase != PH_WARMUP && phase != PH_READY) || !(uw->T > 0.0) || !(uw->T < INFINITY)) {
       s_bad = 1;
-    } else {
-      for (long long p = tid; p < L; p += nt) {
-        const uint32_t op = ops[p];
-        if (!op) continue;
-        const int bond = (int)(op >> 11);
-        if (bond >= d.nbonds || !(op & 1u) || (int)((op >> 2) & 0x1FFu) >= d.type_nverts[d.bond_type[bond]])
-          s_bad = 1;
+    } else if (phase != PH_NEW) {
+      // a walker that went through (part of) Carlo.init! sweeps its own opstring and spin state
+      const long long L = uw->L, n = uw->num_operators;
+      if (L < 0 || L > ops_capacity || n < 0 || n > L) {
+        s_bad = 1;
+      } else {
+        for (long long p = tid; p < L; p += nt) {
+          const uint32_t op = ops[p];
+          if (!op) continue;
+          const int bond = (int)(op >> 11);
+          if (bond >= d.nbonds || !(op & 1u) || (int)((op >> 2) & 0x1FFu) >= d.type_nverts[d.bond_type[bond]])
+            s_bad = 1;
+        }
       }
+      for (int i = tid; i < d.nsites; i += nt)
+        if (state[i] >= d.site_dims[i]) s_bad = 1;
     }
-    for (int i = tid; i < d.nsites; i += nt)
-      if (state[i] >= d.site_dims[i]) s_bad = 1;
   }
   __syncthreads();
-  if (s_bad) {
+  if (s_bad || s_unsup) {
     if (tid == 0) {
-      X->status = SSE_ERR_ARG;
-      uw->status = SSE_ERR_ARG;
+      X->status = s_bad ? SSE_ERR_ARG : SSE_ERR_UNSUPPORTED;
+      uw->status = X->status;
     }
     return;
   }
@@ -1966,18 +2027,16 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
   }
   for (int b = tid; b < d.nbonds; b += nt)
     X->bond_info[b] = make_int4(d.bond_sites[2 * b], d.bond_sites[2 * b + 1], d.bond_type[b], 0);
-  for (int i = tid; i < s_sizes[0]; i += nt) {
-    const int vc = d.diag_vertex[i];
-    X->diag_vc[i] = -1;
-    if (vc < 0) continue;
-    // find the type owning entry i to locate the vertex's class
-    for (int t = 0; t < d.ntypes; t++) {
-      const int o = d.type_diag_off[t], nst = d.type_dims[2 * t] * d.type_dims[2 * t + 1];
-      if (i >= o && i < o + nst) {
-        const int cls = X->vclass[d.type_vert_off[t] + (vc >> 1)];
-        X->diag_vc[i] = cls >= 0 ? (vc | (cls << 16)) : -1;
-        break;
-      }
+  // diagonal vertices tagged with their weight class, type by type (a later type wins where two
+  // types' ranges overlap, as on the host)
+  for (int i = tid; i < s_sizes[0]; i += nt) X->diag_vc[i] = -1;
+  for (int t = 0; t < d.ntypes; t++) {
+    __syncthreads();
+    const int nst = d.type_dims[2 * t] * d.type_dims[2 * t + 1];
+    for (int st = tid; st < nst; st += nt) {
+      const int i = d.type_diag_off[t] + st;
+      const int vc = d.diag_vertex[i];
+      X->diag_vc[i] = vc >= 0 ? (vc | ((int)X->vclass[d.type_vert_off[t] + (vc >> 1)] << 16)) : -1;
     }
   }
   for (int o = tid; o < s_sizes[3]; o += nt) {
@@ -2001,8 +2060,7 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
       tr.packed1 = -1;
       tr.pad = 0;
     } else {
-      int t = 0;
-      while (t + 1 < d.ntypes && d.type_trans_off[t + 1] <= i) t++;
+      const int t = X->row_owner[i];
       for (int o = st; o < st + cnt; o++) {
         const int leg = X->outc[o].packed & 3;
         X->outc[o].packed = (X->outc[o].packed & 0xFFFFF) | (((leg & 1) ? d.type_dims[2 * t + 1] : d.type_dims[2 * t]) << 20);
@@ -2143,6 +2201,8 @@ extern "C" int sse_sweep_noalloc(const sse_model_desc *model, sse_noalloc_walker
   const DevModel *dm = &X->model;
   DevWalker *dw = &X->walker;
   int *dflags = X->flags;
+  // The shared-memory attribute belongs to the k_walk instantiations the engine launches too.  Changing
+  // it here is safe because the engine sets it again before each of its own launches (choose_launch).
   if (cudaFuncSetAttribute(k_walk<MODE_INIT>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess ||
       cudaFuncSetAttribute(k_walk<MODE_SWEEP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
     return SSE_ERR_CUDA;

@@ -1,7 +1,7 @@
 """The engine's own kernels, run on the CPU on emulated warps (tests/warp_emu), against the oracle.
 
-The emulated library is built from the engine's device sources with three textual substitutions
-(two PTX statements and the dynamic shared-memory declaration; see tests/warp_emu/build.py).  It
+The emulated library is built from the engine's device sources with two textual substitutions
+(the PTX lane-mask read and the dynamic shared-memory declaration; see tests/warp_emu/build.py).  It
 runs every launch of the C ABI's host code, with the fake CUDA runtime of tests/fake_cuda as device
 memory.  So these tests check the kernels' logic, bit for bit against the oracle, without a GPU:
 the diagonal update, linking, worms, the controller, measurement, cutoff growth, staging, the plain

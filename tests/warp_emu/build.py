@@ -3,9 +3,8 @@ tests/fake_cuda and a host build of the engine's own kernels running on emulated
 
 The kernels are not copied or rewritten by hand.  They are taken from the engine's sources at build
 time: sse_device.cuh whole, and the blocks of sse_engine.cu between its "kernels: begin" /
-"kernels: end" and "noalloc kernels: begin" / "noalloc kernels: end" markers.  Exactly three textual substitutions are applied, each checked to occur:
+"kernels: end" and "noalloc kernels: begin" / "noalloc kernels: end" markers.  Exactly two textual substitutions are applied, each checked to occur:
  - the PTX read of %lanemask_lt becomes the emulated lane mask;
- - the PTX L1 prefetch becomes a no-op;
  - the extern dynamic shared array becomes the emulated block's buffer.
 The generated file is compiled with g++ against cuda_emu.h and emu_runtime.cpp.
 """
@@ -44,7 +43,6 @@ def generate() -> str:
     dev = open(os.path.join(CSRC, "sse_device.cuh")).read()
     dev = substitute_once(dev, 'asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));', "r = emu_lanemask_lt();",
                           "%lanemask_lt read")
-    dev = substitute_once(dev, 'asm volatile("prefetch.global.L1 [%0];" ::"l"(p));', "(void)p;", "L1 prefetch")
     dev = dev.replace("#pragma once", "")
     if "asm" in re.sub(r"//.*", "", dev).split():
         raise RuntimeError("warp emulator build: sse_device.cuh has inline PTX this build does not emulate")

@@ -168,3 +168,9 @@ inline T atomicExch(T *p, T v) {
   *p = v;
   return old;
 }
+template <class T>
+inline T atomicCAS(T *p, T compare, T v) {
+  T old = *p;
+  if (old == compare) *p = v;
+  return old;
+}
