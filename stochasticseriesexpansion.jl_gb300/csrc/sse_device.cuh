@@ -71,8 +71,11 @@ struct DevModel {
 // Scatter tables (src/vertex_data.jl:106-125) with integer thresholds: for
 // r = u53 * 2^-53 (u53 = u >> 11) the reference's test `r < cum` holds
 // exactly when u53 < ceil(cum * 2^53), so the worm compares integers.
-// packed = leg_out | worm_out << 2 | target vertex code << 10 | dim_out << 20,
-// dim_out the dimension of the site of leg_out (the worm's closing test).
+// packed = leg_out | worm_out << 2 | target vertex code << 10 | ((dim_out - worm_out) & 0xFF) << 20,
+// dim_out the dimension of the site of leg_out: the worm closes at the exit leg of its start
+// operator when worm_out == dim_out - worm_0 (src/worms.jl worm_inverse), i.e. when this field
+// equals worm_0 (worm_0 is 1..254, so a table whose worm_out >= dim_out never closes there, as in
+// the reference).
 struct __align__(16) Outcome {
   unsigned long long thr;
   int32_t packed;
@@ -662,23 +665,26 @@ struct ChaseWindow {
 // Steps of one worm run by lane 0 while draws remain in the buffer (src/sse.jl:262-303 with
 // scatter, src/vertex_data.jl:106-125).  Per step: one 32-byte record (its links, code and type
 // info) and the first 16 bytes of one transition row from L1 (threshold and packed outcome of the
-// row's first outcome; the second half only when the first outcome is not taken).  Kept out of
-// line, with its state in a handful of registers, so that the loop does not share the register
-// budget of the worm update's other phases.
+// row's first outcome; the second half only when the first outcome is not taken).
 //
 // The records of the worm's possible next operators are not prefetched: at 4096 walkers the three
 // extra random sector reads per step cost the diagonal and link phases more than the ~110 cycles
 // they save the step (A/B on the 32x32, beta = 16 batch: 75.9k vs 75.4k walker-sweeps/s).
-// Returns the status; sets win.done when the worm closed; win.pos == 64 when the buffer ran dry.
-__device__ __noinline__ int worm_chase(const Trans *__restrict__ trans, const Outcome *__restrict__ outc,
-                                       Rec *__restrict__ rec, const unsigned long long *__restrict__ dbuf,
-                                       Chase *cs, ChaseWindow *win) {
+//
+// CAPPED: the worm can reach its step cap within this window, so every step is counted against
+// `room`; a window (at most 64 steps) that cannot reach it skips the test.
+template <bool CAPPED>
+__device__ __forceinline__ int worm_chase_loop(const Trans *__restrict__ trans, const Outcome *__restrict__ outc,
+                                               Rec *__restrict__ rec, const unsigned long long *__restrict__ dbuf,
+                                               Chase *cs, ChaseWindow *win) {
   int k = cs->k, leg_in = cs->leg_in, wf = cs->wf;
   int4 ra = cs->ra;
   uint32_t op = (uint32_t)cs->rb.x;
   int slot = cs->rb.y, toff = cs->rb.z, tp = cs->rb.w;
   int pos = win->pos;
-  const int k0 = win->k0, l0 = win->l0, wf0 = win->wf0, room = win->room;
+  const int k0 = win->k0, room = win->room;
+  // the closing tests compare (leg, worm) pairs packed as leg | worm << 2
+  const int lw0 = win->l0 | (win->wf0 << 2);
   const int4 *rq = reinterpret_cast<const int4 *>(rec);
   uint32_t *rop = reinterpret_cast<uint32_t *>(rec);  // rec[k].op = rop[8 k + 4]
   int used = 0, status = ST_OK, done = 0;
@@ -708,26 +714,26 @@ __device__ __noinline__ int worm_chase(const Trans *__restrict__ trans, const Ou
       status = ST_INVALID_VERTEX;
       break;
     }
-    const int leg_out = packed & 3;
-    const int wf_out = (packed >> 2) & 0xFF;
-    const int dim_out = (packed >> 20) & 0xFF;
     // the store precedes the next load of the same record, so a revisit sees the new code; the
     // opstring itself is written once after the worms (slot order, coalesced)
     rop[8 * k + 4] = 1u | ((uint32_t)((packed >> 10) & 0x3FF) << 1) | (op & 0xFFFFF800u);
-    if (k == k0 && leg_out == l0 && wf_out == dim_out - wf0) {
+    // closed at the exit leg: the start operator, the start leg, and worm_out == dim_out - worm_0,
+    // i.e. dim_out - worm_out (bits 20..27 of the outcome) == worm_0
+    if (k == k0 && ((packed & 3) | ((packed >> 18) & 0x3FC)) == lw0) {
       done = 1;
       break;
     }
     used++;
-    wf = wf_out;
-    const int link = leg_out == 0 ? ra.x : leg_out == 1 ? ra.y : leg_out == 2 ? ra.z : ra.w;
+    wf = (packed >> 2) & 0xFF;
+    const int l01 = (packed & 1) ? ra.y : ra.x, l23 = (packed & 1) ? ra.w : ra.z;
+    const int link = (packed & 2) ? l23 : l01;
     leg_in = link & 3;
     k = link >> 2;
-    if (k == k0 && leg_in == l0 && wf == wf0) {
+    if (k == k0 && (leg_in | (wf << 2)) == lw0) {
       done = 1;
       break;
     }
-    if (used > room) {  // len0 + used > cap
+    if (CAPPED && used > room) {  // len0 + used > cap
       status = ST_WORM_CAP;
       break;
     }
@@ -747,6 +753,16 @@ __device__ __noinline__ int worm_chase(const Trans *__restrict__ trans, const Ou
   win->pos = pos;
   win->done = done;
   return status;
+}
+
+// Kept out of line, with its state in a handful of registers, so that the chase does not share the
+// register budget of the worm update's other phases.  Returns the status; sets win.done when the
+// worm closed; win.pos == 64 when the buffer ran dry.
+__device__ __noinline__ int worm_chase(const Trans *__restrict__ trans, const Outcome *__restrict__ outc,
+                                       Rec *__restrict__ rec, const unsigned long long *__restrict__ dbuf,
+                                       Chase *cs, ChaseWindow *win) {
+  if (win->room >= 64) return worm_chase_loop<false>(trans, outc, rec, dbuf, cs, win);
+  return worm_chase_loop<true>(trans, outc, rec, dbuf, cs, win);
 }
 
 __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc, uint32_t *__restrict__ ops,

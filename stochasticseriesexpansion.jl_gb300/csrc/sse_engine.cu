@@ -1147,7 +1147,8 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
       if (((outc[o].packed >> 11) & 0x1FF) >= ty.nverts || ((outc[o].packed >> 2) & 0xFF) > ty.maxworm)
         return fail(e, SSE_ERR_ARG, "transition outcome outside its bond type's tables");
       const int dim_out = (outc[o].packed & 1) ? ty.d1 : ty.d0;  // leg_out & 1: the bond's second site
-      outc[o].packed = (outc[o].packed & 0xFFFFF) | (dim_out << 20);
+      const int worm_out = (outc[o].packed >> 2) & 0xFF;
+      outc[o].packed = (outc[o].packed & 0xFFFFF) | (((dim_out - worm_out) & 0xFF) << 20);
     }
     trans[i].thr0 = outc[start].thr;
     trans[i].packed0 = outc[start].packed;
@@ -2063,7 +2064,9 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
       const int t = X->row_owner[i];
       for (int o = st; o < st + cnt; o++) {
         const int leg = X->outc[o].packed & 3;
-        X->outc[o].packed = (X->outc[o].packed & 0xFFFFF) | (((leg & 1) ? d.type_dims[2 * t + 1] : d.type_dims[2 * t]) << 20);
+        const int dim_out = (leg & 1) ? d.type_dims[2 * t + 1] : d.type_dims[2 * t];
+        const int worm_out = (X->outc[o].packed >> 2) & 0xFF;
+        X->outc[o].packed = (X->outc[o].packed & 0xFFFFF) | (((dim_out - worm_out) & 0xFF) << 20);
       }
       tr.thr0 = X->outc[st].thr;
       tr.packed0 = X->outc[st].packed;
