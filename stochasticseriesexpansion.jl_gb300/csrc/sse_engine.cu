@@ -69,6 +69,8 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
   int status = ST_OK;
   uint8_t *sst = smem;
   int32_t *vlast = reinterpret_cast<int32_t *>(smem);
+  // the warp's site table sits just below the staging area
+  SiteTable *tab = reinterpret_cast<SiteTable *>(smem + smem_per_warp - stage_bytes - (int)sizeof(SiteTable));
 
   if (MODE == MODE_INIT) {
     if (phase == PH_NEW) {
@@ -111,7 +113,7 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
         slot_visits += c.L;
         __syncwarp();
         long long t1 = clock64();
-        const long long nrec = build_links(M, c.L, ops, W->rec, W->cidx, W->vfirst, vlast, lane);
+        const long long nrec = build_links(M, c.L, ops, W->rec, W->cidx, W->vfirst, vlast, tab, lane);
         // records that fit the staging budget move to shared memory for the pointer chase
         Rec *wrec = W->rec;
         const bool staged = stage_bytes > 0 && nrec * (long long)sizeof(Rec) <= (long long)stage_bytes;
@@ -236,7 +238,8 @@ __global__ void k_link_debug(const DevModel *models, DevWalker *walkers, int id,
   DevWalker *W = walkers + id;
   const DevModel &M = models[W->model];
   int32_t *vlast = reinterpret_cast<int32_t *>(smem);
-  build_links(M, W->L, W->ops, W->rec, W->cidx, W->vfirst, vlast, lane);
+  SiteTable *tab = reinterpret_cast<SiteTable *>(smem + warp_area_bytes(M.nsites));
+  build_links(M, W->L, W->ops, W->rec, W->cidx, W->vfirst, vlast, tab, lane);
   for (int i = lane; i < M.nsites; i += 32) vlast_out[i] = vlast[i];
 }
 
@@ -678,9 +681,9 @@ int grow_walker(sse_engine *e, int32_t id, long long need) {
 int choose_launch(sse_engine *e, int max_nsites, int nwork, int &wpb, int &grid, int &smem_per_warp, int &stage,
                   bool init) {
   // per warp: spin state (N bytes, diagonal update), per-site link tails (4N, linking), 64 draws (512 B, worms),
-  // then the staging area for the records of small walkers (sweeps only)
+  // the chunk-local site table (1 KB), then the staging area for the records of small walkers (sweeps only)
   stage = init ? 0 : ((e->stage_bytes + 31) & ~31);
-  smem_per_warp = (((std::max(4 * std::max(max_nsites, 1), 512)) + 31) & ~31) + stage;
+  smem_per_warp = warp_area_bytes(max_nsites) + (int)sizeof(SiteTable) + stage;
   wpb = e->warps_per_block > 0 ? e->warps_per_block : 4;
   if (wpb > 4) wpb = 4;  // k_walk is compiled for at most 128 threads per block
   while (wpb > 1 && (size_t)wpb * smem_per_warp > 200 * 1024) wpb >>= 1;
@@ -1483,7 +1486,7 @@ int sse_vertex_list(sse_engine *e, int32_t id, int32_t *vertices, int32_t *v_fir
   Scratch scratch(e);
   rc = scratch.alloc(&d_vl, (size_t)N);
   if (rc) return rc;
-  const size_t smem = (size_t)4 * N;
+  const size_t smem = (size_t)warp_area_bytes(N) + sizeof(SiteTable);
   CUDA_TRY(e, cudaFuncSetAttribute(k_link_debug, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)std::max<size_t>(smem, 48 * 1024)));
   k_link_debug<<<1, 32, smem, e->stream>>>(e->d_models, e->d_walkers, id, d_vl);
@@ -2199,7 +2202,7 @@ extern "C" int sse_sweep_noalloc(const sse_model_desc *model, sse_noalloc_walker
   if (cudaMemcpyFromSymbol(&st, g_noalloc_scratch, sizeof(int), offsetof(NoAllocScratch, status)) != cudaSuccess)
     return SSE_ERR_CUDA;
   if (st != SSE_OK) return st;
-  const int spw = ((std::max(4 * model->nsites, 512)) + 15) & ~15;
+  const int spw = warp_area_bytes(model->nsites) + (int)sizeof(SiteTable);
   const int smem = std::max(spw, 48 * 1024);
   const DevModel *dm = &X->model;
   DevWalker *dw = &X->walker;

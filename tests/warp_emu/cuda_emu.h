@@ -133,6 +133,7 @@ inline std::common_type_t<A, B> min(A a, B b) {
 
 inline int __popc(unsigned x) { return __builtin_popcount(x); }
 inline int __ffs(int x) { return __builtin_ffs(x); }
+inline int __clz(int x) { return x ? __builtin_clz((unsigned)x) : 32; }
 inline unsigned __umulhi(unsigned a, unsigned b) { return (unsigned)(((unsigned long long)a * b) >> 32); }
 inline unsigned long long __umul64hi(unsigned long long a, unsigned long long b) {
   return (unsigned long long)(((unsigned __int128)a * b) >> 64);
@@ -166,6 +167,12 @@ template <class T>
 inline T atomicExch(T *p, T v) {
   T old = *p;
   *p = v;
+  return old;
+}
+template <class T>
+inline T atomicOr(T *p, T v) {
+  T old = *p;
+  *p = old | v;
   return old;
 }
 template <class T>
