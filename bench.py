@@ -55,12 +55,19 @@ def parse():
                     help="sweeps per chain in the CPU baseline sample (about 10 s on 16 cores for the default workload)")
     ap.add_argument("--cpu-threads", type=int, default=0)
     ap.add_argument("--seed", type=int, default=20261203)
+    ap.add_argument("--uneven-therm", type=int, default=150,
+                    help="thermalisation sweeps per walker of the uneven batch (worm-count controller active)")
     ap.add_argument("--profile", action="store_true", help="open a profiler range around the timed steps only")
     ap.add_argument("--serving-requests", type=int, default=200, help="requests in the serving run (0: skip)")
+    ap.add_argument("--serving-sweep-scale", type=float, default=1e-3,
+                    help="--workload serving: factor on the drawn 10^3-10^4 sweeps per request")
+    ap.add_argument("--serving-max-seconds", type=float, default=1200.0,
+                    help="--workload serving: stop admitting requests after this many seconds")
     ap.add_argument("--workload", default="uniform",
-                    choices=["uniform", "single", "uneven", "bilayer", "magnet_bench", "cluster_bench"],
+                    choices=["uniform", "single", "uneven", "bilayer", "serving", "magnet_bench", "cluster_bench"],
                     help="uniform: the headline batch; single: one 8x8 walker at beta=2; uneven: 8192 walkers of "
-                         "mixed sizes and temperatures; bilayer: 2048 S=1 bilayer walkers 48x48; magnet_bench / "
+                         "mixed sizes and temperatures; bilayer: 2048 S=1 bilayer walkers 48x48; serving: the request loop over "
+                         "the serving distribution's full side and beta ranges; magnet_bench / "
                          "cluster_bench: the reference's own whole-job benchmark tasks, batched")
     return ap.parse_args()
 
@@ -258,26 +265,57 @@ def parity_check(S, flat, eng, ids, states, args, nsweeps=5):
                     "cutoff, replay counter and controller compared bit for bit, observables to 1e-12"}
 
 
-def run_serving(args, device):
+def run_serving(args, device, full=False):
     """The request loop: Poisson arrivals at 200 requests/s, continuous batching, p50/p99 time-to-result.
-    The request distribution is the serving workload's, scaled so the run is bounded: side 8-24,
-    beta 0.5-4 and 20-200 sweeps (log-uniform), 1-64 walkers, S=1/2 or 1, square or bilayer."""
+
+    full=False (the default benchmark's serving block): the serving workload's distribution scaled
+    so that the run takes about a minute -- side 8-24, beta 0.5-4 and 20-200 sweeps (log-uniform),
+    1-64 walkers, S=1/2 or 1, square or bilayer.
+
+    full=True (`--workload serving`): the distribution's own ranges -- side 8-64, beta 0.5-64
+    log-uniform, 1-64 walkers, S=1/2 or 1, square or bilayer -- with the drawn 10^3-10^4 sweeps
+    multiplied by `--serving-sweep-scale` (default 1/1000, so 1-10 sweeps), because a single S=1
+    64x64 bilayer walker at beta = 64 needs seconds per sweep (L near 7.5 million slots) and the
+    drawn counts would take hours.  The loop stops admitting at `--serving-max-seconds`; the line
+    says how many requests completed."""
     from sse_gb300.engine import Engine
     from sse_gb300.serving import ServingLoop, draw_requests
 
-    reqs = draw_requests(args.seed, args.serving_requests, rate=200.0, side=(8, 24), beta=(0.5, 4.0),
-                         walkers=(1, 64), sweeps=(20, 200))
+    if full:
+        nreq = args.serving_requests
+        reqs = draw_requests(args.seed, nreq, rate=200.0, side=(8, 64), beta=(0.5, 64.0), walkers=(1, 64),
+                             sweeps=(1000, 10000), sweep_scale=args.serving_sweep_scale)
+        budget = 180 << 30
+        dist = (f"side 8-64, beta 0.5-64 log-uniform, 1-64 walkers, S in {{1/2,1}}, square or bilayer (J_perp=0.5), "
+                f"10^3-10^4 sweeps log-uniform x {args.serving_sweep_scale:g} (at least 1), 20% thermalisation")
+    else:
+        nreq = args.serving_requests
+        reqs = draw_requests(args.seed, nreq, rate=200.0, side=(8, 24), beta=(0.5, 4.0),
+                             walkers=(1, 64), sweeps=(20, 200))
+        budget = 40 << 30
+        dist = ("side 8-24, beta 0.5-4 and sweeps 20-200 log-uniform, 1-64 walkers, S in {1/2,1}, square or bilayer "
+                "(J_perp=0.5), 20% thermalisation")
     eng = Engine(device)
-    loop = ServingLoop(eng, memory_budget=40 << 30, tick_seconds=0.25)
+    loop = ServingLoop(eng, memory_budget=budget, tick_seconds=0.25)
     # warm the model cache (table builds are host work outside the request path)
     for r in reqs:
         loop._model(r.model_key)
-    loop.run(reqs, realtime=True)
+    t0 = time.perf_counter()
+    loop.run(reqs, realtime=True, max_seconds=args.serving_max_seconds if full else float("inf"))
+    wall = time.perf_counter() - t0
     out = loop.summary()
     eng.close()
-    out.update(rate_per_s=200.0, distribution="side 8-24, beta 0.5-4 and sweeps 20-200 log-uniform, 1-64 walkers, "
-               "S in {1/2,1}, square or bilayer (J_perp=0.5), 20% thermalisation, 0.25 s ticks with per-walker "
-               "sweep counts sized by projected cost")
+    done = {r.rid for r in loop.results}
+    out.update(rate_per_s=200.0, requests_drawn=nreq, requests_completed=len(done), wall_seconds=wall,
+               distribution=dist + "; 0.25 s ticks with per-walker sweep counts sized by projected cost",
+               memory_budget_gb=budget >> 30)
+    if full and loop.results:
+        # the completed request with the most projected work per sweep, and its time-to-result
+        byid = {r.rid: r for r in reqs}
+        r, lat = max(((byid[x.rid], x.latency) for x in loop.results),
+                     key=lambda t: t[0].side ** 2 * t[0].beta * (2 if t[0].lattice == "bilayer" else 1) * t[0].S)
+        out["largest_completed"] = {"S": r.S, "lattice": r.lattice, "side": r.side, "beta": round(r.beta, 2),
+                                    "walkers": r.nwalkers, "sweeps": r.nsweeps, "time_to_result_s": round(lat, 2)}
     return out
 
 
@@ -387,6 +425,8 @@ def run_other_workload(args):
         line.update(run_uneven_balanced(S, eng, args, rng))
     elif args.workload == "bilayer":
         line.update(run_bilayer(S, eng, args))
+    elif args.workload == "serving":
+        line.update(run_serving(args, 0, full=True))
     elif args.workload in ("magnet_bench", "cluster_bench"):
         line.update(run_reference_job(S, eng, args))
     eng.close()
@@ -399,6 +439,61 @@ def balanced_counts(cost, kmax=4096):
     long as one sweep of the slowest."""
     cost = np.maximum(np.asarray(cost, dtype=np.float64), 1.0)
     return np.clip(np.rint(cost.max() / cost), 1, kmax).astype(np.int32)
+
+
+class BalancedBlocks:
+    """Cost-balanced sse_sweep_each blocks over a fixed set of walkers.  The counters of every walker
+    (sweeps, device clock cycles, operator-updates = slot visits + worm steps) are read after each
+    block; the next block gives walker i round(c_max / c_i) sweeps."""
+
+    def __init__(self, eng, ids):
+        self.eng, self.ids = eng, np.asarray(ids, dtype=np.int32)
+        self.k = np.ones(len(self.ids), dtype=np.int32)
+        self.stopped = 0
+        self.read()
+
+    def read(self):
+        inf = [self.eng.info(int(i)) for i in self.ids]
+        self.info = inf
+        self.sw = np.array([x["sweeps"] for x in inf], dtype=np.int64)
+        self.cy = np.array([sum(x["phase_cycles"]) for x in inf], dtype=np.float64)
+        self.ou = np.array([x["slot_visits"] + x["worm_steps"] for x in inf], dtype=np.float64)
+
+    def block(self, measure=True, upto=None):
+        """One block (at most `upto - sweeps` sweeps per walker when `upto` is given); returns its
+        device seconds."""
+        from sse_gb300.engine import SSEError
+
+        k = self.k if upto is None else np.minimum(self.k, np.maximum(upto - self.sw, 0)).astype(np.int32)
+        sw, cy = self.sw, self.cy
+        try:
+            self.eng.sweep_each(self.ids, k, measure=measure)
+        except SSEError:
+            # a walker stopped (a measured worm past the step cap): the others finished the block;
+            # the stopped ones leave the set
+            ok = np.array([self.eng.info(int(i))["status"] == 0 for i in self.ids])
+            self.stopped += int((~ok).sum())
+            dev = self.eng.last_timing()[0] / 1e3
+            self.ids, self.k, sw, cy = self.ids[ok], self.k[ok], sw[ok], cy[ok]
+            self.read()
+            return dev
+        dev = self.eng.last_timing()[0] / 1e3
+        self.read()
+        ran = self.sw - sw
+        cost = np.where(ran > 0, (self.cy - cy) / np.maximum(ran, 1), 0.0)
+        if (ran > 0).any():
+            cost = np.where(ran > 0, cost, cost[ran > 0].min())
+            self.k = balanced_counts(cost)
+        return dev
+
+    def thermalise(self, therm):
+        """Blocks until every walker has done `therm` sweeps (the worm-count controller runs in all of
+        them); returns (blocks, device seconds)."""
+        blocks, dev = 0, 0.0
+        while self.sw.min() < therm:
+            dev += self.block(measure=True, upto=therm)
+            blocks += 1
+        return blocks, dev
 
 
 def run_bilayer(S, eng, args):
@@ -426,34 +521,12 @@ def run_bilayer(S, eng, args):
         eng.reserve(ids[beta_of == b], int(1.25 * 13.2 * flat.nsites * b))
     eng.init(ids)
 
-    def counters():
-        inf = [eng.info(int(i)) for i in ids]
-        return (np.array([x["sweeps"] for x in inf], dtype=np.int64),
-                np.array([sum(x["phase_cycles"]) for x in inf], dtype=np.float64),
-                np.array([x["slot_visits"] + x["worm_steps"] for x in inf], dtype=np.float64), inf)
-
-    sw, cy, ou, _ = counters()
-    k = np.ones(nw, dtype=np.int32)
-    blocks = 0
-    therm_dev = 0.0
-    while sw.min() < args.therm:
-        k = np.minimum(k, np.maximum(args.therm - sw, 0)).astype(np.int32)
-        eng.sweep_each(ids, k, measure=True)
-        therm_dev += eng.last_timing()[0] / 1e3
-        sw1, cy1, ou1, _ = counters()
-        k = balanced_counts((cy1 - cy) / np.maximum(sw1 - sw, 1))
-        sw, cy, ou = sw1, cy1, ou1
-        blocks += 1
+    bb = BalancedBlocks(eng, ids)
+    blocks, therm_dev = bb.thermalise(args.therm)
     therm_s = time.perf_counter() - t0
-    dev = 0.0
-    sw_start, ou_start = sw.copy(), ou.copy()
-    per_beta_dev = []
-    for _ in range(args.steps):
-        eng.sweep_each(ids, k, measure=True)
-        dev += eng.last_timing()[0] / 1e3
-        sw1, cy1, ou1, inf = counters()
-        k = balanced_counts((cy1 - cy) / np.maximum(sw1 - sw, 1))
-        sw, cy, ou = sw1, cy1, ou1
+    sw_start, ou_start = bb.sw.copy(), bb.ou.copy()
+    dev = sum(bb.block(measure=True) for _ in range(args.steps))
+    sw, ou, inf, k = bb.sw, bb.ou, bb.info, bb.k
     Ls = np.array([x["L"] for x in inf])
     dsw, dou = sw - sw_start, ou - ou_start
     return dict(
@@ -466,78 +539,58 @@ def run_bilayer(S, eng, args):
                            "operator_updates_per_walker_sweep": float(dou[beta_of == b].sum() / max(dsw[beta_of == b].sum(), 1)),
                            "cutoff_L_median": int(np.median(Ls[beta_of == b]))} for b in betas.tolist()},
         sweeps_per_block_min_median_max=[int(k.min()), int(np.median(k)), int(k.max())],
-        walkers_stopped=int(sum(x["status"] != 0 for x in inf)),
+        walkers_stopped=bb.stopped,
         thermalisation_sweeps_undone_at_worm_cap=int(sum(x["worm_undos"] for x in inf)),
         cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
 
 
 def run_uneven_balanced(S, eng, args, rng):
-    """8192 walkers of S=1/2 Heisenberg square lattices, side L in {8,...,64} and beta in {0.5,...,64}
-    drawn uniformly from a seed.  A step is one cost-balanced block (sse_sweep_each): walker i runs
-    k_i = round(c_max / c_i) sweeps (1 <= k_i <= 4096), c_i its device clock cycles per sweep measured in
-    the previous block, so that every walker works for about as long as one sweep of the slowest; the
-    launch shape and shared-memory staging budget come from sse_autotune_each on such a block."""
-    from sse_gb300.engine import SSEError
+    """The uneven batch / temperature sweep: 8192 walkers of S=1/2 Heisenberg square lattices, side
+    in {8,16,24,32,48,64} and beta in {0.5,1,...,64} drawn uniformly from a seed (opstrings from about
+    100 to 1.5 million slots).  Capacity is reserved up front from the projected cutoff.  The walkers
+    thermalise for `--uneven-therm` sweeps each with the worm-count controller active, in
+    cost-balanced sse_sweep_each blocks (walker i runs round(c_max / c_i) sweeps, c_i its device clock
+    cycles per sweep in the previous block, capped at what it still needs); the autotuner
+    (sse_autotune_each) then picks walkers per block and the shared-memory staging budget on such a
+    block, and `--steps` balanced blocks with measure! are timed."""
+    from sse_gb300.serving import projected_slots
 
     sides, betas = [8, 16, 24, 32, 48, 64], [0.5, 1, 2, 4, 8, 16, 32, 64]
     nw = 8192
+    therm = args.uneven_therm
     pick = [(int(rng.choice(sides)), float(rng.choice(betas))) for _ in range(nw)]
     models = {L: eng.register_model(S.flatten_model(make_model(S, L))) for L in sides}
     ids = np.zeros(nw, dtype=np.int32)
+    t0 = time.perf_counter()
     for L in sides:
         sel = [k for k, (l, _) in enumerate(pick) if l == L]
-        got = eng.create_walkers(models[L], [dict(T=1.0 / pick[k][1], seed=args.seed, stream=k, thermalization=0)
-                                             for k in sel])
+        got = eng.create_walkers(models[L], [dict(T=1.0 / pick[k][1], seed=args.seed, stream=k,
+                                                  thermalization=therm) for k in sel])
         ids[sel] = got
+        for b in betas:
+            sub = np.array([got[j] for j, k in enumerate(sel) if pick[k][1] == b], dtype=np.int32)
+            if len(sub):
+                eng.reserve(sub, projected_slots(0.5, "square", L, b))
     eng.init(ids)
-
-    def counters():
-        inf = [eng.info(int(i)) for i in ids]
-        return (np.array([x["slot_visits"] + x["worm_steps"] for x in inf], dtype=np.float64),
-                np.array([x["sweeps"] for x in inf], dtype=np.int64), np.array([x["L"] for x in inf]),
-                np.array([sum(x["phase_cycles"]) for x in inf], dtype=np.float64))
-
-    def block(k, measure):
-        try:
-            eng.sweep_each(ids, k, measure=measure)
-        except SSEError as err:
-            raise RuntimeError(f"uneven batch: {err}")
-        return eng.last_timing()[0] / 1e3
-
-    t0 = time.perf_counter()
-    _, sw0, _, cy0 = counters()
-    block(np.ones(nw, dtype=np.int32), False)
-    _, sw1, _, cy1 = counters()
-
-    def balanced(sw_a, cy_a, sw_b, cy_b):
-        # device clock cycles per sweep of every walker in the last block (its latency under load)
-        cost = (cy_b - cy_a) / np.maximum(sw_b - sw_a, 1)
-        return np.clip(np.rint(cost.max() / np.maximum(cost, 1.0)), 1, 4096).astype(np.int32)
-
-    k = balanced(sw0, cy0, sw1, cy1)
-    for _ in range(max(args.warmup, 3)):
-        sw0, cy0 = sw1, cy1
-        block(k, False)
-        _, sw1, _, cy1 = counters()
-        k = balanced(sw0, cy0, sw1, cy1)
-    warm_s = time.perf_counter() - t0
-    best_wpb, best_stage, probe_ms = eng.autotune_each(ids, k, measure=False)
-    ou0, sw0, _, cy0 = counters()
-    dev = 0.0
-    ou_start, sw_start = ou0, sw0
-    for _ in range(args.steps):
-        dev += block(k, True)
-        ou1, sw1, Ls, cy1 = counters()
-        k = balanced(sw0, cy0, sw1, cy1)
-        sw0, cy0 = sw1, cy1
-    ws = float((sw1 - sw_start).sum())
-    ou = float((ou1 - ou_start).sum())
+    bb = BalancedBlocks(eng, ids)
+    blocks, therm_dev = bb.thermalise(therm)
+    therm_s = time.perf_counter() - t0
+    best_wpb, best_stage, probe_ms = eng.autotune_each(ids, bb.k, measure=True)
+    bb.read()
+    sw_start, ou_start = bb.sw.copy(), bb.ou.copy()
+    dev = sum(bb.block(measure=True) for _ in range(args.steps))
+    Ls = np.array([x["L"] for x in bb.info])
+    ws = float((bb.sw - sw_start).sum())
+    ou = float((bb.ou - ou_start).sum())
+    k = bb.k
     return dict(config="8192 walkers, S=1/2 Heisenberg square L in {8..64}, beta in {0.5..64} uniform from a seed; "
-                       "cost-balanced blocks (sse_sweep_each)",
-                steps=args.steps, warmup_blocks=max(args.warmup, 3), warmup_seconds=warm_s,
+                       "cost-balanced blocks (sse_sweep_each); thermalised with the worm-count controller active",
+                thermalization_sweeps=therm, thermalization_blocks=blocks, thermalization_seconds_wall=therm_s,
+                thermalization_seconds_device=therm_dev, steps=args.steps,
                 walker_sweeps_per_s=ws / dev, operator_updates_per_s=ou / dev,
                 sweeps_per_block_min_median_max=[int(k.min()), int(np.median(k)), int(k.max())],
                 autotuned_warps_per_block=best_wpb, autotuned_stage_bytes=best_stage,
+                walkers_stopped=bb.stopped,
                 cutoff_L_min_median_max=[int(Ls.min()), int(np.median(Ls)), int(Ls.max())])
 
 

@@ -110,9 +110,11 @@ def projected_sweep_cost(S: float, lattice: str, side: int, beta: float) -> floa
 
 
 def draw_requests(seed: int, count: int, rate: float = 200.0, side=(8, 64), beta=(0.5, 64.0), walkers=(1, 64),
-                  sweeps=(1000, 10000), therm_fraction: float = 0.2):
+                  sweeps=(1000, 10000), therm_fraction: float = 0.2, sweep_scale: float = 1.0):
     """Poisson arrivals (mean `rate` per second) with the request distribution of the serving workload:
-    S in {1/2, 1}, square or bilayer, side uniform, beta and sweeps log-uniform, walkers uniform."""
+    S in {1/2, 1}, square or bilayer, side uniform, beta and sweeps log-uniform, walkers uniform.
+    `sweep_scale` multiplies every drawn sweep count (at least 1 sweep remains), so that a bounded
+    run can keep the distribution's shape."""
     rng = np.random.default_rng(seed)
     t = 0.0
     out = []
@@ -123,7 +125,7 @@ def draw_requests(seed: int, count: int, rate: float = 200.0, side=(8, 64), beta
         sd = int(rng.integers(side[0], side[1] + 1))
         b = float(math.exp(rng.uniform(math.log(beta[0]), math.log(beta[1]))))
         nw = int(rng.integers(walkers[0], walkers[1] + 1))
-        ns = int(round(math.exp(rng.uniform(math.log(sweeps[0]), math.log(sweeps[1])))))
+        ns = max(1, int(round(sweep_scale * math.exp(rng.uniform(math.log(sweeps[0]), math.log(sweeps[1]))))))
         out.append(Request(rid, t, S, lat, sd, b, nw, ns, seed=int(rng.integers(0, 2**62)),
                            thermalization=int(therm_fraction * ns)))
     return out
