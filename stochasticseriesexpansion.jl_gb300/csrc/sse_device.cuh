@@ -110,7 +110,8 @@ struct DevWalker {
   // device arrays
   uint32_t *ops;   // [cap]   opstring
   Rec *rec;        // [cap]   compacted operators + links (rebuilt every sweep)
-  int32_t *cidx;   // [cap]   slot -> compact index or -1
+  int2 *chunk;     // [cap/32] per 32-slot chunk: compact index of its first operator, bitmask of
+                   //          its operator slots (slot p -> operator chunk.x + popc(bits below p))
   int32_t *vfirst; // [nsites] first leg per site (4k + leg) or -1
   uint8_t *state;  // [nsites]
   double *obs_sum;
@@ -605,7 +606,7 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
 // ---------------------------------------------------------------------------
 
 __device__ __noinline__ long long build_links(const DevModel &M, long long L, const uint32_t *__restrict__ ops,
-                                              Rec *__restrict__ rec, int32_t *__restrict__ cidx,
+                                              Rec *__restrict__ rec, int2 *__restrict__ chunk,
                                               int32_t *__restrict__ vfirst, int32_t *vlast, SiteTable *tab,
                                               int lane) {
   const int N = M.nsites;
@@ -632,7 +633,7 @@ __device__ __noinline__ long long build_links(const DevModel &M, long long L, co
     const bool nonid = op != 0u;
     const unsigned mask = __ballot_sync(FULL, nonid);
     const int k = (int)(kbase + __popc(mask & lt));
-    if (inr) cidx[p] = nonid ? k : -1;
+    if (lane == 0) chunk[base >> 5] = make_int2((int)kbase, (int)mask);
     const int a = nonid ? bi_c.x : -1, b = nonid ? bi_c.y : -1, type = bi_c.z;
     // the previous operator of the chunk on each site (its upper leg 2 when the site is its first
     // site, else 3) and whether a later one of the chunk is on the site, from the site table
@@ -823,7 +824,7 @@ __device__ __noinline__ int worm_chase(const Trans *__restrict__ trans, const Ou
 }
 
 __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc, uint32_t *__restrict__ ops,
-                                        Rec *__restrict__ rec, const int32_t *__restrict__ cidx,
+                                        Rec *__restrict__ rec, const int2 *__restrict__ chunk,
                                         const int32_t *__restrict__ vfirst, uint8_t *__restrict__ state,
                                         unsigned long long *dbuf, bool thermalized, double &wlf, bool &have_wlf,
                                         long long &steps, int lane, int cap_factor) {
@@ -844,7 +845,9 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
       draw2(c.seed, c.stream, c.ctr + 2ull * lane, u1, u2);
       const long long pp = (long long)urange0(u1, L);
       const int ll = (int)urange0(u2, 4ull);
-      const int kk = cidx[pp];
+      const int2 ch = chunk[pp >> 5];  // the operator at slot pp, if any (compact index)
+      const unsigned bit = 1u << (pp & 31);
+      const int kk = ((unsigned)ch.y & bit) ? ch.x + __popc((unsigned)ch.y & (bit - 1u)) : -1;
       const unsigned okm = __ballot_sync(FULL, kk >= 0);
       if (okm) {
         const int t = __ffs(okm) - 1;
@@ -922,12 +925,8 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
     total = __dadd_rn(total, (double)len);
   }
 
-  // the operators' final codes back into the opstring (slot order, coalesced)
-  for (long long k = lane; k < c.n; k += 32) {
-    const int2 os = reinterpret_cast<const int2 *>(rec + k)[2];
-    ops[os.y] = (uint32_t)os.x;
-  }
-  __syncwarp();
+  // the operators' final codes are still only in the records: the caller writes them back into the
+  // opstring (write_back_ops, or fused with the measurement in measure_records)
   have_wlf = thermalized && c.n != 0;
   if (have_wlf) wlf = __ddiv_rn(total, (double)c.n);
 
@@ -1122,6 +1121,128 @@ __device__ long long measure_pass_int(const DevModel &M, const Chain &c, DevWalk
   }
   __syncwarp();
   return (long long)(sign < 0 ? 1 : 0);
+}
+
+// The operators' final codes from the compacted records back into the opstring (slot order).
+__device__ __noinline__ void write_back_ops(const Chain &c, const Rec *__restrict__ rec, uint32_t *__restrict__ ops,
+                                            int lane) {
+  for (long long k = lane; k < c.n; k += 32) {
+    const int2 os = reinterpret_cast<const int2 *>(rec + k)[2];
+    ops[os.y] = (uint32_t)os.x;
+  }
+  __syncwarp();
+}
+
+// measure_pass_int over the compacted records instead of the opstring: the non-identity operators
+// in slot order, n entries instead of L slots (identity slots add no term to any sum).  With
+// `first` the pass also writes every operator's code back into the opstring and counts the sign.
+template <int NE>
+__device__ long long measure_pass_rec(const DevModel &M, const Chain &c, DevWalker *W, const Rec *__restrict__ rec,
+                                      uint32_t *__restrict__ ops, const uint8_t *__restrict__ state, int e0,
+                                      bool first, double sign_in, int lane) {
+  const long long n = c.n;
+  const int N = M.nsites, md = M.maxdim;
+  const int4 *__restrict__ bond_info = M.bond_info;
+  const DevType *__restrict__ types = M.types;
+  const int8_t *__restrict__ vsign = M.sign;
+  const uint8_t *__restrict__ leg_state = M.leg_state;
+  const int2 *__restrict__ r2 = reinterpret_cast<const int2 *>(rec);  // r2[4 k + 2] = (op, slot) of record k
+  const int32_t *__restrict__ cf[2];
+  int t0[2], carry[2];
+  long long s1[2], s2[2], s3[2];
+  unsigned __int128 s4[2];
+#pragma unroll
+  for (int q = 0; q < NE; q++) {
+    cf[q] = M.est_coef2 + (long long)(e0 + q) * N * md;
+    int acc = 0;
+    for (int i = lane; i < N; i += 32) acc += cf[q][(long long)i * md + state[i]];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(FULL, acc, o);
+    t0[q] = acc;
+    carry[q] = acc;
+    s1[q] = s2[q] = s3[q] = 0;
+    s4[q] = 0;
+  }
+  long long negs = 0;
+  int2 os_n = (lane < n) ? r2[4 * (long long)lane + 2] : make_int2(0, 0);
+  for (long long base = 0; base < n; base += 32) {
+    const int2 os = os_n;
+    os_n = (base + 32 + lane < n) ? r2[4 * (base + 32 + lane) + 2] : make_int2(0, 0);
+    const uint32_t op = (uint32_t)os.x;  // 0 past the last operator
+    if (first && op != 0u) ops[os.y] = op;
+    int d[2] = {0, 0};
+    if (op != 0u) {
+      const int4 bi = __ldg(bond_info + (op >> 11));
+      const int vo = types[bi.z].vert_off + (int)((op >> 2) & 0x1FFu);
+      if (first) negs += vsign[vo] < 0;
+      if (!(op & 2u)) {
+        const uchar4 ls = *reinterpret_cast<const uchar4 *>(leg_state + 4 * vo);
+#pragma unroll
+        for (int q = 0; q < NE; q++) {
+          d[q] = (cf[q][(long long)bi.x * md + ls.z] - cf[q][(long long)bi.x * md + ls.x]) +
+                 (cf[q][(long long)bi.y * md + ls.w] - cf[q][(long long)bi.y * md + ls.y]);
+        }
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NE; q++) {
+      int x = d[q];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
+      }
+      const int t = carry[q] + x;
+      if (op != 0u) {
+        const long long tl = t;
+        s1[q] += tl;
+        s2[q] += tl < 0 ? -tl : tl;
+        const long long t2 = tl * tl;
+        s3[q] += t2;
+        s4[q] += (unsigned __int128)((unsigned long long)t2) * (unsigned long long)t2;
+      }
+      carry[q] = __shfl_sync(FULL, t, 31);
+    }
+  }
+  if (first) negs = warp_sum_i64(negs);
+  const double sign = first ? ((negs & 1) ? -1.0 : 1.0) : sign_in;
+  if (first && lane == 0) observe_base(M, c, W, sign);
+#pragma unroll
+  for (int q = 0; q < NE; q++) {
+    const long long S1 = warp_sum_i64(s1[q]), S2 = warp_sum_i64(s2[q]), S3 = warp_sum_i64(s3[q]);
+    const unsigned __int128 S4 = warp_sum_u128(s4[q]);
+    if (lane == 0) {
+      const long long a = t0[q];
+      const long long a2 = a * a;
+      const double mag = __dmul_rn(__ll2double_rn(a + S1), 0.5);
+      const double absmag = __dmul_rn(__ll2double_rn((a < 0 ? -a : a) + S2), 0.5);
+      const double mag2 = __dmul_rn(__ll2double_rn(a2 + S3), 0.25);
+      const double mag4 = __dmul_rn(u128_to_double(S4 + (unsigned __int128)((unsigned long long)a2) * (unsigned long long)a2),
+                                    0.0625);
+      finish_estimator(M, c, W, e0 + q, sign, mag, absmag, mag2, mag4);
+    }
+  }
+  __syncwarp();
+  return (long long)(sign < 0 ? 1 : 0);
+}
+
+// measure! (exact integer estimators, M.est_int) right after the worm update, on the compacted
+// records, fused with writing the operators' codes back into the opstring.
+__device__ __noinline__ void measure_records(const DevModel &M, const Chain &c, DevWalker *W,
+                                             const Rec *__restrict__ rec, uint32_t *__restrict__ ops,
+                                             const uint8_t *__restrict__ state, int lane) {
+  if (M.nest == 0) {
+    measure_pass_rec<0>(M, c, W, rec, ops, state, 0, true, 1.0, lane);
+    return;
+  }
+  double sign = 1.0;
+  for (int e0 = 0; e0 < M.nest; e0 += 2) {
+    const bool first = e0 == 0;
+    long long neg;
+    if (M.nest - e0 >= 2) neg = measure_pass_rec<2>(M, c, W, rec, ops, state, e0, first, sign, lane);
+    else neg = measure_pass_rec<1>(M, c, W, rec, ops, state, e0, first, sign, lane);
+    if (first) sign = neg ? -1.0 : 1.0;
+  }
 }
 
 __device__ __noinline__ void measure(const DevModel &M, const Chain &c, DevWalker *W, const uint32_t *__restrict__ ops,

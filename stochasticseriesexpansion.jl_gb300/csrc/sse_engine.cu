@@ -113,7 +113,7 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
         slot_visits += c.L;
         __syncwarp();
         long long t1 = clock64();
-        const long long nrec = build_links(M, c.L, ops, W->rec, W->cidx, W->vfirst, vlast, tab, lane);
+        const long long nrec = build_links(M, c.L, ops, W->rec, W->chunk, W->vfirst, vlast, tab, lane);
         // records that fit the staging budget move to shared memory for the pointer chase
         Rec *wrec = W->rec;
         const bool staged = stage_bytes > 0 && nrec * (long long)sizeof(Rec) <= (long long)stage_bytes;
@@ -127,18 +127,29 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
         long long t2 = clock64();
         double wlf = 0.0;
         bool have_wlf = false;
-        status = worm_update(M, c, wc, ops, wrec, W->cidx, W->vfirst, state,
+        status = worm_update(M, c, wc, ops, wrec, W->chunk, W->vfirst, state,
                              reinterpret_cast<unsigned long long *>(smem), thermalized, wlf, have_wlf, worm_steps,
                              lane, W->cap_factor);
-        if (status == ST_WORM_UNDONE) {  // rare: counted straight in the walker record
+        // an undone worm phase (thermalisation only) leaves the opstring as the diagonal update made it
+        const bool undone = status == ST_WORM_UNDONE;
+        if (undone) {  // rare: counted straight in the walker record
           status = ST_OK;
           if (lane == 0) W->worm_undos++;
         }
         if (status != ST_OK) break;
+        long long t3 = clock64();
+        // measure! after this sweep (Carlo measures once sweeps > thermalization); the records still
+        // hold the operators' final codes, and the exact integer measurement runs on them while
+        // writing the codes back into the opstring
+        // writing the codes back into the opstring.  The sweep at sweeps == thermalization can undo its
+        // worm phase and still be measured: it measures the opstring the diagonal update left.
+        const bool meas = (flags & SSE_SWEEP_MEASURE) && sweeps + 1 > therm;
+        const bool fused = meas && M.est_int && !undone;
+        if (fused) measure_records(M, c, W, wrec, ops, state, lane);
+        else if (!undone) write_back_ops(c, wrec, ops, lane);
         if (have_wlf && lane == 0) observe(W, 5, wlf);
         sweeps++;
-        long long t3 = clock64();
-        if ((flags & SSE_SWEEP_MEASURE) && sweeps > therm) measure(M, c, W, ops, state, lane);
+        if (meas && !fused) measure(M, c, W, ops, state, lane);
         __syncwarp();
         long long t4 = clock64();
         cyc0 += t1 - t0;
@@ -214,7 +225,7 @@ struct GrowEntry {
   int32_t id, pad;
   uint32_t *ops;
   Rec *rec;
-  int32_t *cidx;
+  int2 *chunk;
   long long cap;
 };
 
@@ -225,7 +236,7 @@ __global__ void k_apply_growth(DevWalker *walkers, const GrowEntry *g, int n) {
     DevWalker *W = walkers + g[i].id;
     W->ops = g[i].ops;
     W->rec = g[i].rec;
-    W->cidx = g[i].cidx;
+    W->chunk = g[i].chunk;
     W->cap = g[i].cap;
     if (W->status == ST_NEED_GROW) W->status = ST_OK;
     W->need_L = 0;
@@ -239,7 +250,7 @@ __global__ void k_link_debug(const DevModel *models, DevWalker *walkers, int id,
   const DevModel &M = models[W->model];
   int32_t *vlast = reinterpret_cast<int32_t *>(smem);
   SiteTable *tab = reinterpret_cast<SiteTable *>(smem + warp_area_bytes(M.nsites));
-  build_links(M, W->L, W->ops, W->rec, W->cidx, W->vfirst, vlast, tab, lane);
+  build_links(M, W->L, W->ops, W->rec, W->chunk, W->vfirst, vlast, tab, lane);
   for (int i = lane; i < M.nsites; i += 32) vlast_out[i] = vlast[i];
 }
 
@@ -458,7 +469,7 @@ struct HostWalker {
   long long cap = 0;
   uint32_t *ops = nullptr;
   Rec *rec = nullptr;
-  int32_t *cidx = nullptr;
+  int2 *chunk = nullptr;  // chunk index: one entry per 32 slots
   int32_t *vfirst = nullptr;
   uint8_t *state = nullptr;
   double *obs_sum = nullptr, *obs_last = nullptr;
@@ -524,6 +535,9 @@ void dev_free(sse_engine *e, T *&p) {
   p = nullptr;
 }
 
+// Entries of a walker's chunk index for `cap` opstring slots: one per 32-slot chunk.
+size_t chunk_count(long long cap) { return (size_t)((cap + 31) / 32); }
+
 // Device buffers of one call, freed (stream-ordered) when the call returns, on every path.
 struct Scratch {
   sse_engine *e;
@@ -568,7 +582,7 @@ int upload(sse_engine *e, HostModel &hm, const T *src, size_t count, const T **d
 void free_walker_buffers(sse_engine *e, HostWalker &h) {
   dev_free(e, h.ops);
   dev_free(e, h.rec);
-  dev_free(e, h.cidx);
+  dev_free(e, h.chunk);
   dev_free(e, h.vfirst);
   dev_free(e, h.state);
   dev_free(e, h.obs_sum);
@@ -642,14 +656,14 @@ int grow_walker(sse_engine *e, int32_t id, long long need) {
   if (cap >= (1LL << 31) / 4) return fail(e, SSE_ERR_CAPACITY, "walker opstring exceeds 2^29 slots");
   uint32_t *ops = nullptr;
   Rec *rec = nullptr;
-  int32_t *cidx = nullptr;
+  int2 *chunk = nullptr;
   rc = dev_alloc(e, &ops, (size_t)cap);
   if (!rc) rc = dev_alloc(e, &rec, (size_t)cap);
-  if (!rc) rc = dev_alloc(e, &cidx, (size_t)cap);
+  if (!rc) rc = dev_alloc(e, &chunk, chunk_count(cap));
   if (rc) {
     dev_free(e, ops);
     dev_free(e, rec);
-    dev_free(e, cidx);
+    dev_free(e, chunk);
     return rc;
   }
   if (h.ops && w.L > 0) {
@@ -658,20 +672,20 @@ int grow_walker(sse_engine *e, int32_t id, long long need) {
     if (st != cudaSuccess) {
       dev_free(e, ops);
       dev_free(e, rec);
-      dev_free(e, cidx);
+      dev_free(e, chunk);
       return fail(e, SSE_ERR_CUDA, std::string("cudaMemcpyAsync (opstring prefix): ") + cudaGetErrorString(st));
     }
   }
   dev_free(e, h.ops);
   dev_free(e, h.rec);
-  dev_free(e, h.cidx);
+  dev_free(e, h.chunk);
   h.ops = ops;
   h.rec = rec;
-  h.cidx = cidx;
+  h.chunk = chunk;
   h.cap = cap;
   w.ops = ops;
   w.rec = rec;
-  w.cidx = cidx;
+  w.chunk = chunk;
   w.cap = cap;
   if (w.status == ST_NEED_GROW) w.status = ST_OK;
   w.need_L = 0;
@@ -832,17 +846,17 @@ int run_until_done(sse_engine *e, int mode, std::vector<int32_t> work, long long
         g.id = work[i];
         rc = dev_alloc(e, &g.ops, (size_t)cap);
         if (!rc) rc = dev_alloc(e, &g.rec, (size_t)cap);
-        if (!rc) rc = dev_alloc(e, &g.cidx, (size_t)cap);
+        if (!rc) rc = dev_alloc(e, &g.chunk, chunk_count(cap));
         if (rc) return rc;
         if (h.ops)
           CUDA_TRY(e, cudaMemcpyAsync(g.ops, h.ops, sizeof(uint32_t) * (size_t)h.cap, cudaMemcpyDeviceToDevice,
                                       e->stream));
         dev_free(e, h.ops);
         dev_free(e, h.rec);
-        dev_free(e, h.cidx);
+        dev_free(e, h.chunk);
         h.ops = g.ops;
         h.rec = g.rec;
-        h.cidx = g.cidx;
+        h.chunk = g.chunk;
         h.cap = cap;
         g.cap = cap;
         grow.push_back(g);
@@ -1233,7 +1247,7 @@ int sse_walkers_create(sse_engine *e, int32_t model_id, int32_t count, const sse
     h.cap = std::max<long long>(256, ((2 * cutoff + 100) + 63) & ~63LL);
     rc = dev_alloc(e, &h.ops, (size_t)h.cap);
     if (!rc) rc = dev_alloc(e, &h.rec, (size_t)h.cap);
-    if (!rc) rc = dev_alloc(e, &h.cidx, (size_t)h.cap);
+    if (!rc) rc = dev_alloc(e, &h.chunk, chunk_count(h.cap));
     if (!rc) rc = dev_alloc(e, &h.vfirst, (size_t)hm.nsites);
     if (!rc) rc = dev_alloc(e, &h.state, (size_t)hm.nsites);
     if (!rc) rc = dev_alloc(e, &h.obs_sum, (size_t)hm.nobs);
@@ -1249,7 +1263,7 @@ int sse_walkers_create(sse_engine *e, int32_t model_id, int32_t count, const sse
     memset(&w, 0, sizeof w);
     w.ops = h.ops;
     w.rec = h.rec;
-    w.cidx = h.cidx;
+    w.chunk = h.chunk;
     w.vfirst = h.vfirst;
     w.state = h.state;
     w.obs_sum = h.obs_sum;
@@ -1841,7 +1855,7 @@ namespace {
 // ==== noalloc kernels: begin (device code only down to the matching end marker) ====
 struct NoAllocScratch {
   Rec rec[SSE_NOALLOC_MAX_SLOTS];
-  int32_t cidx[SSE_NOALLOC_MAX_SLOTS];
+  int2 chunk[SSE_NOALLOC_MAX_SLOTS / 32];
   int32_t vfirst[SSE_NOALLOC_MAX_SITES];
   int4 bond_info[SSE_NOALLOC_MAX_BONDS];
   Trans trans[SSE_NOALLOC_MAX_TRANSITIONS];
@@ -2107,7 +2121,7 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
     memset(&w, 0, sizeof w);
     w.ops = ops;
     w.rec = X->rec;
-    w.cidx = X->cidx;
+    w.chunk = X->chunk;
     w.vfirst = X->vfirst;
     w.state = state;
     w.obs_sum = obs_sum;

@@ -193,32 +193,36 @@ def test_emulated_worm_cap_stop_matches_oracle(S, O, eng):
     assert eng.info(int(ids[1]))["sweeps"] == 3 and eng.info(int(ids[1]))["status"] == 0
 
 
-@pytest.mark.parametrize("stage", [0, 192 * 1024])
-def test_emulated_worm_cap_undo_matches_oracle(S, O, eng, stage):
+@pytest.mark.parametrize("stage,therm", [(0, None), (192 * 1024, None), (0, 1)])
+def test_emulated_worm_cap_undo_matches_oracle(S, O, eng, stage, therm):
     """The same worm in a thermalisation sweep: the kernels undo the sweep's worm phase exactly as
     the oracle does (records in global memory, and staged in shared memory), and the walker sweeps
-    on bit for bit."""
+    on bit for bit.  With thermalization = 1 the long worm falls in the last thermalisation sweep
+    (sweeps == thermalization): its worm phase is undone with the controller still active, and that
+    sweep is nevertheless measured, on the opstring the diagonal update left."""
     from test_worm_cap import FACTOR, LONG_WORM, THERMALISING, long_worm_model
 
+    therm = THERMALISING if therm is None else therm
+    measured = therm < THERMALISING
     flat = long_worm_model(S)
     mid = eng.register_model(flat)
-    params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=THERMALISING)
+    params = [dict(T=1 / LONG_WORM["beta"], seed=LONG_WORM["seed"], stream=s, thermalization=therm)
               for s in (LONG_WORM["stream"], 0)]
     ids = eng.create_walkers(mid, params)
     eng.set_worm_cap(ids, FACTOR)
     eng.init(ids)
     eng.set_staging(stage)
     try:
-        eng.sweep(ids, 5, measure=False)
+        eng.sweep(ids, 5, measure=measured)
     finally:
         eng.set_staging(0)
     om = O.OracleModel(flat)
     for p, wid in zip(params, ids.tolist()):
-        w = O.OracleWalker(om, T=p["T"], seed=p["seed"], stream=p["stream"], thermalization=THERMALISING)
+        w = O.OracleWalker(om, T=p["T"], seed=p["seed"], stream=p["stream"], thermalization=therm)
         w.w.worm_cap_factor = FACTOR
         w.init()
-        w.run(5, measure=False)
-        compare(eng, flat, wid, w, measured=False)
+        w.run(5, measure=measured)
+        compare(eng, flat, wid, w, measured=measured)
         assert eng.info(wid)["worm_undos"] == w.w.worm_undos
     assert eng.info(int(ids[0]))["worm_undos"] == 1
     assert eng.check(ids).tolist() == [0, 0]
