@@ -265,7 +265,7 @@ int sse_sweep_tempering(sse_engine *eng, int32_t nladders, int32_t nrungs, const
  * synchronisation of cudaMalloc/cudaFree.  The caller owns every input and
  * output buffer in device memory; the per-sweep scratch (compacted operator
  * records, slot index, per-site heads) and the tables derived from the model
- * live in one static device array of about 12 MB (its size follows from the
+ * live in one static device array of about 13 MB (its size follows from the
  * SSE_NOALLOC_MAX_* limits below), which every GPU that loads this library
  * holds until the process exits.
  *

@@ -422,8 +422,11 @@ __device__ __forceinline__ void diag_stage_a(DiagStage &a, uint32_t op, bool inr
   if (a.kind) a.bi = __ldg(bond_info + a.bond);
 }
 
+// thr: 1 KB of the warp's shared memory (the site table's, idle during this phase) for the per-class
+// thresholds: thr[2c] = (insert surely / insert never), thr[2c + 1] = (remove surely / remove never).
 __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *__restrict__ ops, uint8_t *sst,
-                                        bool thermalized, long long &resize_count, long long &need_L, int lane) {
+                                        ulonglong2 *thr, bool thermalized, long long &resize_count,
+                                        long long &need_L, int lane) {
   if (2 * c.n >= c.L) {
     const long long Lnew = c.L + c.L / 2 + 100;  // floor(1.5 L + 100)
     if (Lnew > c.cap) {
@@ -453,9 +456,8 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
   const bool use_thr = ncls <= 32;
   const double wc = (use_thr && lane < ncls) ? M.cls_w[lane] : 0.0;
 
-  // per-class integer thresholds (lane c holds class c), valid while |n - n_c| <= 16
+  // per-class integer thresholds (in thr[], written by lane c for class c), valid while |n - n_c| <= 16
   long long n_c = -(1ll << 60);
-  unsigned long long ti_a = 0, ti_r = U53_ALL, tr_a = 0, tr_r = U53_ALL;
 
   // two chunks of opcodes in flight, the first chunk's stage A done before the loop
   uint32_t op_n1 = (lane < L) ? ops[lane] : 0u;
@@ -520,16 +522,23 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
       n_c = n;
       if (lane < ncls) {
         const long long nlo = n_c - 48, nhi = n_c + 48;
-        ti_a = thr_lt(__dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nlo)), wc));
-        ti_r = (L - nhi > 0) ? thr_lt(__dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nhi)), wc)) : U53_ALL;
-        tr_a = thr_mul_lt(wc, __dmul_rn((double)(L - nhi + 1), premove_raw), 0ull);
-        tr_r = thr_mul_lt(wc, __dmul_rn((double)(L - nlo + 1), premove_raw), U53_ALL);
+        const unsigned long long ti_a = thr_lt(__dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nlo)), wc));
+        const unsigned long long ti_r =
+            (L - nhi > 0) ? thr_lt(__dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nhi)), wc)) : U53_ALL;
+        const unsigned long long tr_a = thr_mul_lt(wc, __dmul_rn((double)(L - nhi + 1), premove_raw), 0ull);
+        const unsigned long long tr_r = thr_mul_lt(wc, __dmul_rn((double)(L - nlo + 1), premove_raw), U53_ALL);
+        thr[2 * lane] = make_ulonglong2(ti_a, ti_r);
+        thr[2 * lane + 1] = make_ulonglong2(tr_a, tr_r);
       }
+      __syncwarp();
     }
     // classify: surely accepted / surely rejected / maybe
-    const int src = cls >= 0 ? cls : 0;
-    const unsigned long long a_ins = __shfl_sync(FULL, ti_a, src), r_ins = __shfl_sync(FULL, ti_r, src);
-    const unsigned long long a_rem = __shfl_sync(FULL, tr_a, src), r_rem = __shfl_sync(FULL, tr_r, src);
+    ulonglong2 ti = make_ulonglong2(0ull, U53_ALL), tr = make_ulonglong2(0ull, U53_ALL);
+    if (use_thr && cls >= 0) {
+      ti = thr[2 * cls];
+      tr = thr[2 * cls + 1];
+    }
+    const unsigned long long a_ins = ti.x, r_ins = ti.y, a_rem = tr.x, r_rem = tr.y;
     const long long nlo = n - __popc(dgm & lt);
     const long long nhi = n + __popc(idm & lt);
     bool alo = false, ahi = false;

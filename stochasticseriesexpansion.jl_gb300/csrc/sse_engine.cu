@@ -88,7 +88,7 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
     while (phase == PH_WARMUP && warmup_done < W->warmup) {
       for (int i = lane; i < N; i += 32) sst[i] = state[i];
       __syncwarp();
-      status = diag_update(M, c, ops, sst, false, resize_count, need_L, lane);
+      status = diag_update(M, c, ops, sst, reinterpret_cast<ulonglong2 *>(tab), false, resize_count, need_L, lane);
       if (status != ST_OK) break;
       slot_visits += c.L;
       warmup_done++;
@@ -108,7 +108,8 @@ __device__ void process_walker(const DevModel &M, DevWalker *W, uint8_t *smem, i
         long long t0 = clock64();
         for (int i = lane; i < N; i += 32) sst[i] = state[i];
         __syncwarp();
-        status = diag_update(M, c, ops, sst, thermalized, resize_count, need_L, lane);
+        status = diag_update(M, c, ops, sst, reinterpret_cast<ulonglong2 *>(tab), thermalized, resize_count, need_L,
+                             lane);
         if (status != ST_OK) break;
         slot_visits += c.L;
         __syncwarp();

@@ -46,12 +46,16 @@ struct alignas(16) uint4 {
 struct alignas(4) uchar4 {
   unsigned char x, y, z, w;
 };
+struct alignas(16) ulonglong2 {
+  unsigned long long x, y;
+};
 static_assert(sizeof(int2) == 8 && sizeof(uint2) == 8 && sizeof(int4) == 16 && sizeof(uint4) == 16, "layout");
 static_assert(sizeof(uchar4) == 4 && alignof(uchar4) == 4, "layout");
 inline int2 make_int2(int x, int y) { return int2{x, y}; }
 inline uint2 make_uint2(unsigned x, unsigned y) { return uint2{x, y}; }
 inline int4 make_int4(int x, int y, int z, int w) { return int4{x, y, z, w}; }
 inline uint4 make_uint4(unsigned x, unsigned y, unsigned z, unsigned w) { return uint4{x, y, z, w}; }
+inline ulonglong2 make_ulonglong2(unsigned long long x, unsigned long long y) { return ulonglong2{x, y}; }
 
 struct EmuDim3 {
   unsigned x, y, z;
