@@ -701,6 +701,9 @@ def main():
         blk = min(100, args.therm - done)
         eng.sweep(ids, blk, measure=True)
         done += blk
+    # walkers per block and the shared-memory staging budget from the autotuner (its probes are
+    # real Carlo steps of the thermalised batch)
+    tuned_wpb, tuned_stage, _ = eng.autotune(ids, nsweeps_probe=5, measure=True)
     # the sweep blocks run as CUDA-graph replays (the first warm-up step captures the block)
     for _ in range(args.warmup):
         eng.sweep(ids, args.sweeps_per_step, measure=True, graph=True)
@@ -822,6 +825,8 @@ def main():
                 "parallelism": f"replicas x{world}",
                 "l2": f"working set {sum(x['capacity'] for x in info1) * 40 / 1e9:.1f} GB of walker state, larger than L2",
                 "mean_cutoff_L": mean_L,
+                "autotuned_walkers_per_block": tuned_wpb,
+                "autotuned_stage_bytes": tuned_stage,
             },
             "operator_updates_per_s": opupd,
             "phase_cycle_share": phases,
