@@ -62,7 +62,9 @@ struct DevModel {
   const double *cls_w;      // weight of each class
   int32_t ncls, pad2, pad3, pad4;
   const int32_t *est_coef2;  // 2 * est_coef as integers when est_int (every coefficient a multiple of 1/2)
-  int32_t est_int, pad5, pad6, pad7;
+  int32_t est_int;
+  int32_t one_worm;  // every bond type has maxworm 1 (one worm type): the chase's row index needs no worm
+  int32_t pad6, pad7;
   const struct Trans *trans;  // one per (type, vertex, leg_in, worm_in)
   const struct Outcome *outc;
   const double *est_coef;
@@ -740,7 +742,9 @@ struct ChaseWindow {
 //
 // CAPPED: the worm can reach its step cap within this window, so every step is counted against
 // `room`; a window (at most 64 steps) that cannot reach it skips the test.
-template <bool CAPPED>
+// ONE_WORM: every bond type has a single worm type (maxworm 1, e.g. every S=1/2 model), so the worm
+// is always 1 and the row of (vertex, leg) needs no worm term.
+template <bool CAPPED, bool ONE_WORM>
 __device__ __forceinline__ int worm_chase_loop(const Trans *__restrict__ trans, const Outcome *__restrict__ outc,
                                                Rec *__restrict__ rec, const unsigned long long *__restrict__ dbuf,
                                                Chase *cs, ChaseWindow *win) {
@@ -758,7 +762,8 @@ __device__ __forceinline__ int worm_chase_loop(const Trans *__restrict__ trans, 
   while (pos < 64) {
     const unsigned long long u53 = dbuf[pos];
     pos++;
-    const int ti = toff + ((int)((op >> 2) & 0x1FFu) * 4 + leg_in) * (tp & 0xFF) + (wf - 1);
+    const int ti = ONE_WORM ? toff + (int)((op >> 2) & 0x1FFu) * 4 + leg_in
+                            : toff + ((int)((op >> 2) & 0x1FFu) * 4 + leg_in) * (tp & 0xFF) + (wf - 1);
     const int4 *tr = reinterpret_cast<const int4 *>(trans + ti);
     const int4 h0 = __ldg(tr);  // thr0, packed0, rest
     int packed = h0.z;
@@ -791,12 +796,12 @@ __device__ __forceinline__ int worm_chase_loop(const Trans *__restrict__ trans, 
       break;
     }
     used++;
-    wf = (packed >> 2) & 0xFF;
+    if (!ONE_WORM) wf = (packed >> 2) & 0xFF;
     const int l01 = (packed & 1) ? ra.y : ra.x, l23 = (packed & 1) ? ra.w : ra.z;
     const int link = (packed & 2) ? l23 : l01;
     leg_in = link & 3;
     k = link >> 2;
-    if (k == k0 && (leg_in | (wf << 2)) == lw0) {
+    if (k == k0 && (ONE_WORM ? leg_in == (lw0 & 3) : (leg_in | (wf << 2)) == lw0)) {
       done = 1;
       break;
     }
@@ -827,9 +832,13 @@ __device__ __forceinline__ int worm_chase_loop(const Trans *__restrict__ trans, 
 // worm closed; win.pos == 64 when the buffer ran dry.
 __device__ __noinline__ int worm_chase(const Trans *__restrict__ trans, const Outcome *__restrict__ outc,
                                        Rec *__restrict__ rec, const unsigned long long *__restrict__ dbuf,
-                                       Chase *cs, ChaseWindow *win) {
-  if (win->room >= 64) return worm_chase_loop<false>(trans, outc, rec, dbuf, cs, win);
-  return worm_chase_loop<true>(trans, outc, rec, dbuf, cs, win);
+                                       Chase *cs, ChaseWindow *win, bool one_worm) {
+  if (one_worm) {
+    if (win->room >= 64) return worm_chase_loop<false, true>(trans, outc, rec, dbuf, cs, win);
+    return worm_chase_loop<true, true>(trans, outc, rec, dbuf, cs, win);
+  }
+  if (win->room >= 64) return worm_chase_loop<false, false>(trans, outc, rec, dbuf, cs, win);
+  return worm_chase_loop<true, false>(trans, outc, rec, dbuf, cs, win);
 }
 
 __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc, uint32_t *__restrict__ ops,
@@ -904,7 +913,7 @@ __device__ __noinline__ int worm_update(const DevModel &M, Chain &c, WormCtl &wc
         win.wf0 = wf0;
         win.room = (cap - cs.len) > 0x3FFFFFFFLL ? 0x3FFFFFFF : (int)(cap - cs.len);
         win.done = 0;
-        status = worm_chase(M.trans, M.outc, rec, dbuf, &cs, &win);
+        status = worm_chase(M.trans, M.outc, rec, dbuf, &cs, &win, M.one_worm != 0);
         pos = win.pos;
         done = win.done != 0;
       }

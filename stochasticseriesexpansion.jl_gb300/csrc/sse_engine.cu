@@ -1113,6 +1113,9 @@ int sse_model_register(sse_engine *e, const sse_model_desc *d, int32_t *model_id
     }
   }
   m.ncls = (int32_t)cls_w.size();
+  m.one_worm = 1;
+  for (int t = 0; t < d->ntypes; t++)
+    if (types[t].maxworm != 1) m.one_worm = 0;
   if (cls_w.empty()) cls_w.push_back(0.0);
   if (!rc) rc = upload(e, hm, diag_vc.data(), ndiag, &m.diag_vc);
   if (!rc) rc = upload(e, hm, vclass.data(), nvert, &m.vclass);
