@@ -139,8 +139,9 @@ def make_model(S, side):
 
 
 def walker_bytes(L, W, N):
-    """Algorithmic DRAM bytes of one walker-sweep: diagonal update r+w 4L, linking r 4L + w 16L,
-    slot index w 4L, worm 12 B per step (link r, opcode r+w), state r+w 4N+4N."""
+    """Algorithmic DRAM bytes of one walker-sweep: diagonal update r+w 4L, linking r 4L + w 16L (the
+    compacted records), 4L of slot bookkeeping (the chunk index and writing the operators' final codes
+    back), worm 12 B per step (link r, opcode r+w), state r+w 4N+4N."""
     return 28.0 * L + 12.0 * W + 8.0 * N
 
 
@@ -421,6 +422,29 @@ def run_other_workload(args):
                     gpu_plain_sweeps_per_s=500 / plain_s, gpu_graph_replay_sweeps_per_s=500 / (graph_ms / 1e3),
                     cpu_oracle_one_core_sweeps_per_s=n / cpu_s,
                     mean_L=eng.info(int(a))["L"])
+        # the same model batched: 4096 walkers in one persistent launch, against the oracle with one
+        # chain per host core (both after 2000 thermalisation sweeps)
+        nb = 4096
+        bids = eng.create_walkers(mid, [dict(T=0.5, seed=args.seed, stream=100 + k, thermalization=2000)
+                                        for k in range(nb)])
+        eng.init(bids)
+        eng.sweep(bids, 2000, measure=False)
+        eng.sweep(bids, 200, measure=True)
+        bms = []
+        for _ in range(3):
+            eng.sweep(bids, 200, measure=True)
+            bms.append(eng.last_timing()[0])
+        nthreads = args.cpu_threads or os.cpu_count() or 1
+        chains = [O.OracleWalker(om, T=0.5, seed=args.seed, stream=100 + k, thermalization=2000)
+                  for k in range(nthreads)]
+        for w in chains:
+            w.init()
+        O.run_parallel(om, chains, 2000, measure=False, nthreads=nthreads)
+        t0 = time.perf_counter()
+        O.run_parallel(om, chains, n, measure=True, nthreads=nthreads)
+        cpu_all = nthreads * n / (time.perf_counter() - t0)
+        line.update(batched_walkers=nb, gpu_batched_walker_sweeps_per_s=nb * 200 * 3 / (sum(bms) / 1e3),
+                    cpu_oracle_all_cores_walker_sweeps_per_s=cpu_all, cpu_threads=nthreads)
     elif args.workload == "uneven":
         line.update(run_uneven_balanced(S, eng, args, rng))
     elif args.workload == "bilayer":
