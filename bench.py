@@ -63,6 +63,8 @@ def parse():
                     help="--workload serving: factor on the drawn 10^3-10^4 sweeps per request")
     ap.add_argument("--serving-max-seconds", type=float, default=1200.0,
                     help="--workload serving: stop admitting requests after this many seconds")
+    ap.add_argument("--serving-request-budget", type=float, default=60.0,
+                    help="--workload serving: refuse a request whose projected device time exceeds this")
     ap.add_argument("--workload", default="uniform",
                     choices=["uniform", "single", "uneven", "bilayer", "serving", "magnet_bench", "cluster_bench"],
                     help="uniform: the headline batch; single: one 8x8 walker at beta=2; uneven: 8192 walkers of "
@@ -277,8 +279,10 @@ def run_serving(args, device, full=False):
     log-uniform, 1-64 walkers, S=1/2 or 1, square or bilayer -- with the drawn 10^3-10^4 sweeps
     multiplied by `--serving-sweep-scale` (default 1/1000, so 1-10 sweeps), because a single S=1
     64x64 bilayer walker at beta = 64 needs seconds per sweep (L near 7.5 million slots) and the
-    drawn counts would take hours.  The loop stops admitting at `--serving-max-seconds`; the line
-    says how many requests completed."""
+    drawn counts would take hours.  Requests whose projected device time (the worm-count controller's
+    transient included, serving.projected_request_seconds) exceeds `--serving-request-budget` are
+    refused at admission and counted; the loop stops at `--serving-max-seconds`; the line says how many
+    requests completed."""
     from sse_gb300.engine import Engine
     from sse_gb300.serving import ServingLoop, draw_requests
 
@@ -288,7 +292,8 @@ def run_serving(args, device, full=False):
                              sweeps=(1000, 10000), sweep_scale=args.serving_sweep_scale)
         budget = 180 << 30
         dist = (f"side 8-64, beta 0.5-64 log-uniform, 1-64 walkers, S in {{1/2,1}}, square or bilayer (J_perp=0.5), "
-                f"10^3-10^4 sweeps log-uniform x {args.serving_sweep_scale:g} (at least 1), 20% thermalisation")
+                f"10^3-10^4 sweeps log-uniform x {args.serving_sweep_scale:g} (at least 1), 20% thermalisation; "
+                f"requests projected over {args.serving_request_budget:g} s of device time refused at admission")
     else:
         nreq = args.serving_requests
         reqs = draw_requests(args.seed, nreq, rate=200.0, side=(8, 24), beta=(0.5, 4.0),
@@ -297,7 +302,8 @@ def run_serving(args, device, full=False):
         dist = ("side 8-24, beta 0.5-4 and sweeps 20-200 log-uniform, 1-64 walkers, S in {1/2,1}, square or bilayer "
                 "(J_perp=0.5), 20% thermalisation")
     eng = Engine(device)
-    loop = ServingLoop(eng, memory_budget=budget, tick_seconds=0.25)
+    loop = ServingLoop(eng, memory_budget=budget, tick_seconds=0.25,
+                       max_request_seconds=args.serving_request_budget if full else None)
     # warm the model cache (table builds are host work outside the request path)
     for r in reqs:
         loop._model(r.model_key)
@@ -553,6 +559,28 @@ def run_bilayer(S, eng, args):
     sw, ou, inf, k = bb.sw, bb.ou, bb.info, bb.k
     Ls = np.array([x["L"] for x in inf])
     dsw, dou = sw - sw_start, ou - ou_start
+    # the CPU restatement on the same tables: 16 GPU walkers (every beta) exported and swept once on
+    # the host cores, one chain per thread
+    from oracle import oracle as O
+
+    om = O.OracleModel(flat)
+    nthreads = args.cpu_threads or os.cpu_count() or 1
+    chains = []
+    for j in range(min(nthreads, len(bb.ids))):
+        wid = int(bb.ids[(j * len(bb.ids)) // min(nthreads, len(bb.ids))])
+        ops, st, winf = eng.export(wid)
+        w = O.OracleWalker(om, T=winf["T"], seed=args.seed, stream=0, thermalization=args.therm)
+        w.set_opstring(ops, winf["num_operators"])
+        w.set_state(st)
+        w.w.ctr, w.w.num_worms, w.w.avg_worm_length, w.w.sweeps = (winf["rng_counter"], winf["num_worms"],
+                                                                   winf["avg_worm_length"], winf["sweeps"])
+        chains.append(w)
+    t0 = time.perf_counter()
+    O.run_parallel(om, chains, 1, measure=True, nthreads=nthreads)
+    cpu_s = time.perf_counter() - t0
+    cpu_ou = sum(w.w.worm_steps_total + w.w.slot_visits_total for w in chains)
+    nops = np.array([x["num_operators"] for x in inf], dtype=np.float64)
+    wsteps = np.array([x["worm_steps"] for x in inf], dtype=np.float64)
     return dict(
         config="2048 walkers, S=1 square bilayer 48x48 (4608 sites), J=1, J_perp=0.5, Dz=0.3, hz=0.2, "
                "beta in {4,8,16} (a third each); cost-balanced sse_sweep_each blocks",
@@ -561,7 +589,14 @@ def run_bilayer(S, eng, args):
         walker_sweeps_per_s=float(dsw.sum()) / dev, operator_updates_per_s=float(dou.sum()) / dev,
         per_beta={str(b): {"walker_sweeps_per_s": float(dsw[beta_of == b].sum()) / dev,
                            "operator_updates_per_walker_sweep": float(dou[beta_of == b].sum() / max(dsw[beta_of == b].sum(), 1)),
-                           "cutoff_L_median": int(np.median(Ls[beta_of == b]))} for b in betas.tolist()},
+                           "cutoff_L_median": int(np.median(Ls[beta_of == b])),
+                           "operators_median": int(np.median(nops[beta_of == b]))} for b in betas.tolist()},
+        regime=("the worm-count controller's transient: the reference's controller starts from an average worm "
+                "length of 1 and adapts by 1% per sweep, so for many sweeps every sweep runs tens to hundreds of "
+                "times the equilibrium 2n worm steps; operator-updates/s is the comparable rate"),
+        cpu_baseline={"value": cpu_ou / cpu_s, "unit": "operator-updates/s", "cores": nthreads, "kind": "port",
+                      "sample": f"{len(chains)} GPU walkers (all betas) exported and swept once on the host cores, "
+                                "one chain per thread"},
         sweeps_per_block_min_median_max=[int(k.min()), int(np.median(k)), int(k.max())],
         walkers_stopped=bb.stopped,
         thermalisation_sweeps_undone_at_worm_cap=int(sum(x["worm_undos"] for x in inf)),

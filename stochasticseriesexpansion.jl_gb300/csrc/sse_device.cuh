@@ -637,7 +637,6 @@ __device__ __noinline__ long long build_links(const DevModel &M, long long L, co
   int4 bi_c = op_c ? __ldg(bond_info + (op_c >> 11)) : make_int4(-1, -1, 0, 0);
   for (long long base = 0; base < L; base += 32) {
     const long long p = base + lane;
-    const bool inr = p < L;
     const uint32_t op_nn = (base + 64 + lane < L) ? ops[base + 64 + lane] : 0u;
     const int4 bi_n = op_n ? __ldg(bond_info + (op_n >> 11)) : make_int4(-1, -1, 0, 0);
     const uint32_t op = op_c;

@@ -13,6 +13,7 @@ unmeasured).  The loop
   arrive while others run join the next launch,
 * retires a request as soon as its walkers are done, reporting its
   observables and its time-to-result (completion - arrival),
+* refuses, when given a bound, a request whose projected device time exceeds it,
 * replaces a walker that the engine stopped (a worm past the step cap,
   SSE_ERR_WORM_CAP) with a fresh chain, up to `retries` times per walker:
   slot k of a request runs stream k, its a-th replacement stream
@@ -109,6 +110,20 @@ def projected_sweep_cost(S: float, lattice: str, side: int, beta: float) -> floa
     return 4.2 * projected_operators(S, lattice, side, beta) + 100
 
 
+def projected_request_seconds(req, step_seconds: float = 1.2e-6) -> float:
+    """Device seconds one walker of `req` is projected to need, bounded from the expensive side.
+
+    A fresh walker runs the reference's worm-count controller transient (src/sse.jl:204-217): the
+    average worm length starts at 1 and rises by 1 % per sweep, so once the cutoff has grown, every
+    sweep runs far more worm steps than the equilibrium 2n.  On the oracle, 64x64 S=1/2 at beta = 64
+    ran 35-55 x 2n steps per sweep over its first 30 sweeps, and the 48x48 S=1 bilayer at beta = 4
+    and 16 ran 60-145 x 2n.  The projection takes 80 n (S=1/2) or 240 n (S=1) dependent worm steps
+    per sweep at `step_seconds` each (one warp chases one walker; about 1.2 us per step at full load)."""
+    n = projected_operators(req.S, req.lattice, req.side, req.beta)
+    per_sweep = (80.0 if req.S == 0.5 else 240.0) * n * step_seconds
+    return req.nsweeps * per_sweep
+
+
 def draw_requests(seed: int, count: int, rate: float = 200.0, side=(8, 64), beta=(0.5, 64.0), walkers=(1, 64),
                   sweeps=(1000, 10000), therm_fraction: float = 0.2, sweep_scale: float = 1.0):
     """Poisson arrivals (mean `rate` per second) with the request distribution of the serving workload:
@@ -150,8 +165,14 @@ class ServingLoop:
     it every walker gets `tick_sweeps` sweeps per tick."""
 
     def __init__(self, engine, memory_budget: int, tick_sweeps: int = 10, clock=time.perf_counter,
-                 tick_seconds: float | None = None, walker_rate: float = 1.5e6, retries: int = 2):
+                 tick_seconds: float | None = None, walker_rate: float = 1.5e6, retries: int = 2,
+                 max_request_seconds: float | None = None):
+        """`max_request_seconds`: refuse, at admission, a request whose projected device time
+        (projected_request_seconds) exceeds it: a kernel cannot be interrupted inside a sweep, so one
+        admitted request whose sweeps take minutes would stall every request batched with it."""
         self.eng = engine
+        self.max_request_seconds = max_request_seconds
+        self.refused: list = []
         self.retries = int(retries)
         self.budget = int(memory_budget)
         self.tick = int(tick_sweeps)
@@ -184,6 +205,10 @@ class ServingLoop:
         admitted = []
         while self.pending:
             req = self.pending[0]
+            if self.max_request_seconds is not None and projected_request_seconds(req) > self.max_request_seconds:
+                self.pending.pop(0)
+                self.refused.append(req.rid)
+                continue
             need = req.nwalkers * projected_walker_bytes(req.S, req.lattice, req.side, req.beta)
             if self.active and self.used + need > self.budget:
                 break
@@ -314,6 +339,7 @@ class ServingLoop:
         span = max((r.finish for r in self.results), default=0.0)
         return {
             "requests": len(self.results),
+            "refused": len(self.refused),
             "failed": sum(r.status != "ok" for r in self.results),
             "walkers_replaced": sum(r.replaced for r in self.results),
             "thermalisation_sweeps_undone": sum(r.undone for r in self.results),

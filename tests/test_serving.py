@@ -165,3 +165,20 @@ def test_cost_aware_ticks_give_small_walkers_more_sweeps(S):
     assert loop.rate != 1e6
     for r in res:
         assert np.all(r.sums[:, 0] == 400)
+
+
+def test_admission_refuses_requests_over_the_projected_time_budget(S):
+    """With max_request_seconds, a request whose projected device time exceeds it is refused at
+    admission (counted, never run); the others run as usual."""
+    from sse_gb300.serving import Request, ServingLoop, projected_request_seconds
+
+    eng = FakeEngine()
+    small = Request(0, 0.0, 0.5, "square", 8, 1.0, nwalkers=2, nsweeps=10, seed=1)
+    big = Request(1, 0.0, 1.0, "bilayer", 64, 64.0, nwalkers=4, nsweeps=5, seed=2)
+    assert projected_request_seconds(small) < 1.0 < 60.0 < projected_request_seconds(big)
+    loop = ServingLoop(eng, memory_budget=1 << 40, tick_sweeps=10, clock=iter(np.arange(0, 1e6, 0.5)).__next__,
+                       max_request_seconds=60.0)
+    res = loop.run([small, big], realtime=False)
+    assert [r.rid for r in res] == [0] and loop.refused == [1]
+    assert loop.summary()["refused"] == 1
+    assert all(len(ids) == 2 for ids, _ in eng.calls)  # the big request's walkers were never created
