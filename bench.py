@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--therm", type=int, default=2000, help="thermalisation sweeps before the warm-up steps")
     ap.add_argument("--sweeps-per-step", type=int, default=50)
     ap.add_argument("--plain-walkers", type=int, default=8)
+    ap.add_argument("--wpb", type=int, default=0,
+                    help="walkers (warps) per block of the sweep launch, staging off; 0: the autotuner chooses")
     ap.add_argument("--cpu-sweeps", type=int, default=2000,
                     help="sweeps per chain in the CPU baseline sample (about 10 s on 16 cores for the default workload)")
     ap.add_argument("--cpu-threads", type=int, default=0)
@@ -762,7 +764,11 @@ def main():
         done += blk
     # walkers per block and the shared-memory staging budget from the autotuner (its probes are
     # real Carlo steps of the thermalised batch)
-    tuned_wpb, tuned_stage, _ = eng.autotune(ids, nsweeps_probe=5, measure=True)
+    if args.wpb:
+        eng.set_launch(args.wpb, 0)
+        tuned_wpb, tuned_stage = args.wpb, 0
+    else:
+        tuned_wpb, tuned_stage, _ = eng.autotune(ids, nsweeps_probe=5, measure=True)
     # the sweep blocks run as CUDA-graph replays (the first warm-up step captures the block)
     for _ in range(args.warmup):
         eng.sweep(ids, args.sweeps_per_step, measure=True, graph=True)
