@@ -481,8 +481,23 @@ class BalancedBlocks:
     def __init__(self, eng, ids):
         self.eng, self.ids = eng, np.asarray(ids, dtype=np.int32)
         self.k = np.ones(len(self.ids), dtype=np.int32)
+        self.cost = np.ones(len(self.ids))  # last measured clock cycles per sweep of every walker
         self.stopped = 0
         self.read()
+        self.reset_totals()
+
+    def reset_totals(self):
+        """Start counting the sweeps and operator-updates of the following blocks, per walker id (a walker
+        that stops keeps what it did in the blocks before)."""
+        self.done_sw = {int(i): 0 for i in self.ids}
+        self.done_ou = {int(i): 0.0 for i in self.ids}
+
+    def _count(self, ids, sw0, ou0):
+        pos = {int(i): j for j, i in enumerate(self.ids)}
+        for i, a, b in zip(ids.tolist(), sw0.tolist(), ou0.tolist()):
+            if i in pos:
+                self.done_sw[i] += int(self.sw[pos[i]] - a)
+                self.done_ou[i] += float(self.ou[pos[i]] - b)
 
     def read(self):
         inf = [self.eng.info(int(i)) for i in self.ids]
@@ -497,7 +512,7 @@ class BalancedBlocks:
         from sse_gb300.engine import SSEError
 
         k = self.k if upto is None else np.minimum(self.k, np.maximum(upto - self.sw, 0)).astype(np.int32)
-        sw, cy = self.sw, self.cy
+        ids0, sw, cy, ou = self.ids, self.sw, self.cy, self.ou
         try:
             self.eng.sweep_each(self.ids, k, measure=measure)
         except SSEError:
@@ -506,16 +521,17 @@ class BalancedBlocks:
             ok = np.array([self.eng.info(int(i))["status"] == 0 for i in self.ids])
             self.stopped += int((~ok).sum())
             dev = self.eng.last_timing()[0] / 1e3
-            self.ids, self.k, sw, cy = self.ids[ok], self.k[ok], sw[ok], cy[ok]
+            self.ids, self.k, self.cost, sw, cy = self.ids[ok], self.k[ok], self.cost[ok], sw[ok], cy[ok]
             self.read()
+            self._count(ids0[ok], sw, ou[ok])
             return dev
         dev = self.eng.last_timing()[0] / 1e3
         self.read()
+        self._count(ids0, sw, ou)
         ran = self.sw - sw
-        cost = np.where(ran > 0, (self.cy - cy) / np.maximum(ran, 1), 0.0)
-        if (ran > 0).any():
-            cost = np.where(ran > 0, cost, cost[ran > 0].min())
-            self.k = balanced_counts(cost)
+        # walkers that ran no sweep in this block (done with thermalisation) keep their last cost
+        self.cost = np.where(ran > 0, (self.cy - cy) / np.maximum(ran, 1), self.cost)
+        self.k = balanced_counts(self.cost)
         return dev
 
     def thermalise(self, therm):
@@ -556,11 +572,13 @@ def run_bilayer(S, eng, args):
     bb = BalancedBlocks(eng, ids)
     blocks, therm_dev = bb.thermalise(args.therm)
     therm_s = time.perf_counter() - t0
-    sw_start, ou_start = bb.sw.copy(), bb.ou.copy()
+    bb.reset_totals()
     dev = sum(bb.block(measure=True) for _ in range(args.steps))
-    sw, ou, inf, k = bb.sw, bb.ou, bb.info, bb.k
+    inf, k = bb.info, bb.k
     Ls = np.array([x["L"] for x in inf])
-    dsw, dou = sw - sw_start, ou - ou_start
+    live_beta = np.array([1.0 / x["T"] for x in inf])
+    dsw = np.array([bb.done_sw[int(i)] for i in ids], dtype=np.float64)
+    dou = np.array([bb.done_ou[int(i)] for i in ids], dtype=np.float64)
     # the CPU restatement on the same tables: 16 GPU walkers (every beta) exported and swept once on
     # the host cores, one chain per thread
     from oracle import oracle as O
@@ -582,7 +600,6 @@ def run_bilayer(S, eng, args):
     cpu_s = time.perf_counter() - t0
     cpu_ou = sum(w.w.worm_steps_total + w.w.slot_visits_total for w in chains)
     nops = np.array([x["num_operators"] for x in inf], dtype=np.float64)
-    wsteps = np.array([x["worm_steps"] for x in inf], dtype=np.float64)
     return dict(
         config="2048 walkers, S=1 square bilayer 48x48 (4608 sites), J=1, J_perp=0.5, Dz=0.3, hz=0.2, "
                "beta in {4,8,16} (a third each); cost-balanced sse_sweep_each blocks",
@@ -591,8 +608,8 @@ def run_bilayer(S, eng, args):
         walker_sweeps_per_s=float(dsw.sum()) / dev, operator_updates_per_s=float(dou.sum()) / dev,
         per_beta={str(b): {"walker_sweeps_per_s": float(dsw[beta_of == b].sum()) / dev,
                            "operator_updates_per_walker_sweep": float(dou[beta_of == b].sum() / max(dsw[beta_of == b].sum(), 1)),
-                           "cutoff_L_median": int(np.median(Ls[beta_of == b])),
-                           "operators_median": int(np.median(nops[beta_of == b]))} for b in betas.tolist()},
+                           "cutoff_L_median": int(np.median(Ls[live_beta == b])),
+                           "operators_median": int(np.median(nops[live_beta == b]))} for b in betas.tolist()},
         regime=("the worm-count controller's transient: the reference's controller starts from an average worm "
                 "length of 1 and adapts by 1% per sweep, so for many sweeps every sweep runs tens to hundreds of "
                 "times the equilibrium 2n worm steps; operator-updates/s is the comparable rate"),
@@ -638,11 +655,11 @@ def run_uneven_balanced(S, eng, args, rng):
     therm_s = time.perf_counter() - t0
     best_wpb, best_stage, probe_ms = eng.autotune_each(ids, bb.k, measure=True)
     bb.read()
-    sw_start, ou_start = bb.sw.copy(), bb.ou.copy()
+    bb.reset_totals()
     dev = sum(bb.block(measure=True) for _ in range(args.steps))
     Ls = np.array([x["L"] for x in bb.info])
-    ws = float((bb.sw - sw_start).sum())
-    ou = float((bb.ou - ou_start).sum())
+    ws = float(sum(bb.done_sw.values()))
+    ou = float(sum(bb.done_ou.values()))
     k = bb.k
     return dict(config="8192 walkers, S=1/2 Heisenberg square L in {8..64}, beta in {0.5..64} uniform from a seed; "
                        "cost-balanced blocks (sse_sweep_each); thermalised with the worm-count controller active",

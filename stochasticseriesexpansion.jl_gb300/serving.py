@@ -114,14 +114,24 @@ def projected_request_seconds(req, step_seconds: float = 1.2e-6) -> float:
     """Device seconds one walker of `req` is projected to need, bounded from the expensive side.
 
     A fresh walker runs the reference's worm-count controller transient (src/sse.jl:204-217): the
-    average worm length starts at 1 and rises by 1 % per sweep, so once the cutoff has grown, every
-    sweep runs far more worm steps than the equilibrium 2n.  On the oracle, 64x64 S=1/2 at beta = 64
-    ran 35-55 x 2n steps per sweep over its first 30 sweeps, and the 48x48 S=1 bilayer at beta = 4
-    and 16 ran 60-145 x 2n.  The projection takes 80 n (S=1/2) or 240 n (S=1) dependent worm steps
-    per sweep at `step_seconds` each (one warp chases one walker; about 1.2 us per step at full load)."""
-    n = projected_operators(req.S, req.lattice, req.side, req.beta)
-    per_sweep = (80.0 if req.S == 0.5 else 240.0) * n * step_seconds
-    return req.nsweeps * per_sweep
+    average worm length starts at 1 and rises by 1 % per sweep, so every sweep runs far more worm
+    steps than the equilibrium 2n.  On the oracle, 64x64 S=1/2 at beta = 64 ran 35-55 x 2n steps per
+    sweep over its first 30 sweeps, the 48x48 S=1 bilayer at beta = 4 and 16 ran 60-145 x 2n.  Its
+    operator count meanwhile grows with the cutoff: about 10-30 N T after Carlo.init!'s diagonal
+    sweeps, then about 1.5x per sweep up to the equilibrium n.  The projection takes sweep k to hold
+    min(n_eq, 15 N T 1.5^k) operators and to run 100 (S=1/2) or 260 (S=1) worm steps per operator,
+    each a dependent step of `step_seconds` (one warp chases one walker; about 1.2 us at full load)."""
+    n_eq = projected_operators(req.S, req.lattice, req.side, req.beta)
+    nsites = req.side * req.side * (2 if req.lattice == "bilayer" else 1)
+    per_op = 100.0 if req.S == 0.5 else 260.0
+    total = 0.0
+    for k in range(req.nsweeps):
+        n_k = min(n_eq, 15.0 * nsites / req.beta * 1.5 ** k)
+        total += per_op * n_k
+        if n_k >= n_eq:
+            total += per_op * n_eq * (req.nsweeps - k - 1)
+            break
+    return total * step_seconds
 
 
 def draw_requests(seed: int, count: int, rate: float = 200.0, side=(8, 64), beta=(0.5, 64.0), walkers=(1, 64),

@@ -174,7 +174,7 @@ def test_admission_refuses_requests_over_the_projected_time_budget(S):
 
     eng = FakeEngine()
     small = Request(0, 0.0, 0.5, "square", 8, 1.0, nwalkers=2, nsweeps=10, seed=1)
-    big = Request(1, 0.0, 1.0, "bilayer", 64, 64.0, nwalkers=4, nsweeps=5, seed=2)
+    big = Request(1, 0.0, 1.0, "bilayer", 64, 8.0, nwalkers=4, nsweeps=10, seed=2)
     assert projected_request_seconds(small) < 1.0 < 60.0 < projected_request_seconds(big)
     loop = ServingLoop(eng, memory_budget=1 << 40, tick_sweeps=10, clock=iter(np.arange(0, 1e6, 0.5)).__next__,
                        max_request_seconds=60.0)
