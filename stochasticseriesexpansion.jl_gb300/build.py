@@ -22,7 +22,10 @@ NVCC_FLAGS = [
     "-lineinfo",
     "-O3",
     "-std=c++17",
-    # accept/reject and controller arithmetic must not be contracted into FMAs
+    # accept/reject and controller arithmetic must not be contracted into FMAs.  The flag governs
+    # floating-point contraction only (integer and address arithmetic still use fused multiply-adds);
+    # a -fmad=true build gave bit-identical chains at the same speed, so it stays as a guard for
+    # FP64 code written without the explicit *_rn intrinsics
     "-fmad=false",
     "-Xcompiler", "-fPIC,-ffp-contract=off",
     "-shared",

@@ -2118,6 +2118,8 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
     m.vclass = X->vclass;
     m.cls_w = X->cls_w;
     m.ncls = s_ncls;
+    m.one_worm = 0;  // the general chase and slot-order measurement paths
+    m.est_int = 0;
     m.trans = X->trans;
     m.outc = X->outc;
     m.est_coef = d.est_coef;

@@ -17,9 +17,25 @@ DEPS = SOURCES + [os.path.join(ROOT, "stochasticseriesexpansion.jl_gb300", "csrc
                   os.path.join(ROOT, "include", "sse_gpu.h")]
 
 
+def _up_to_date() -> bool:
+    return os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in DEPS)
+
+
 def build() -> str:
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in DEPS):
+    if _up_to_date():
         return LIB
+    os.makedirs(os.path.dirname(LIB), exist_ok=True)
+    import fcntl
+
+    # pytest-xdist workers build at the same time: one builds, the others wait and reuse its library
+    with open(LIB + ".lock", "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not _up_to_date():
+            _build_locked()
+    return LIB
+
+
+def _build_locked() -> None:
     import importlib.util
 
     spec = importlib.util.spec_from_file_location(
@@ -32,4 +48,3 @@ def build() -> str:
     cmd = [nvcc, *flags, "-cudart", "none", "-I", os.path.join(ROOT, "include"), "-o", LIB + ".tmp", *SOURCES]
     subprocess.run(cmd, check=True)
     os.replace(LIB + ".tmp", LIB)
-    return LIB

@@ -71,11 +71,26 @@ def generate() -> str:
     )
 
 
+def _up_to_date() -> bool:
+    return os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in DEPS + [
+        os.path.join(HERE, "emu_dispatch.inc")])
+
+
 def build() -> str:
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(d) for d in DEPS + [
-            os.path.join(HERE, "emu_dispatch.inc")]):
+    if _up_to_date():
         return LIB
     os.makedirs(BUILD, exist_ok=True)
+    import fcntl
+
+    # pytest-xdist workers build at the same time: one builds, the others wait and reuse its library
+    with open(os.path.join(BUILD, ".lock"), "w") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        if not _up_to_date():
+            _build_locked()
+    return LIB
+
+
+def _build_locked() -> None:
     src = os.path.join(BUILD, "emu_kernels.cpp")
     with open(src, "w") as f:
         f.write(generate())
@@ -99,7 +114,6 @@ def build() -> str:
     subprocess.run([nvcc, *flags, "-cudart", "none", "-I", os.path.join(ROOT, "include"), "-o", LIB + ".tmp",
                     os.path.join(CSRC, "sse_engine.cu"), os.path.join(FAKE, "fake_cudart.cpp"), *objs], check=True)
     os.replace(LIB + ".tmp", LIB)
-    return LIB
 
 
 if __name__ == "__main__":
