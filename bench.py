@@ -35,8 +35,14 @@ import numpy as np  # noqa: E402
 
 import _sse_loader  # noqa: E402
 
-WORKLOAD = "4096 walkers, S=1/2 Heisenberg, 32x32 periodic square (2048 bonds), beta=16"
 METRIC = "walker-sweeps/s"
+
+
+def workload_name(args):
+    """The headline workload with the sizes this run uses; the defaults give "4096 walkers, S=1/2
+    Heisenberg, 32x32 periodic square (2048 bonds), beta=16"."""
+    return (f"{args.walkers} walkers, S=1/2 Heisenberg, {args.side}x{args.side} periodic square "
+            f"({2 * args.side * args.side} bonds), beta={args.beta:g}")
 
 
 def parse():
@@ -360,7 +366,7 @@ def run_reference(args):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt * 1e3 / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "i32+f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "walkers_per_step": len(walkers), "sweeps_per_step": per_step,
+        "config": {"workload": workload_name(args), "walkers_per_step": len(walkers), "sweeps_per_step": per_step,
                    "note": "CPU restatement of the reference sweep (Julia reference not runnable here)"},
         "cpu_baseline": {"value": value, "unit": METRIC, "cores": nthreads, "kind": "port",
                          "sample": f"{len(walkers)} chains x {per_step} sweeps per step after 300 thermalisation sweeps"},
@@ -898,7 +904,7 @@ def main():
             "dtype": "i32+f64",
             "data": "synthetic",
             "config": {
-                "workload": WORKLOAD,
+                "workload": workload_name(args),
                 "walkers": nw,
                 "side": args.side,
                 "beta": args.beta,
