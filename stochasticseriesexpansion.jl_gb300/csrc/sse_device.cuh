@@ -364,10 +364,9 @@ __device__ unsigned long long thr_mul_lt(double w, double P, unsigned long long 
 }
 
 struct DiagStage {  // per-lane data of one chunk after the first pipeline stage
-  uint32_t op;
-  int kind;  // 0 none, 1 identity, 2 diagonal, 3 off-diagonal
+  uint32_t opb;  // the opcode, or for an identity slot its drawn bond << 11
+  int kind;      // 0 none, 1 identity, 2 diagonal, 3 off-diagonal
   unsigned long long u53;
-  uint32_t bond;
   int4 bi;
 };
 
@@ -377,22 +376,19 @@ struct DiagStage {  // per-lane data of one chunk after the first pipeline stage
 // shuffles.  At most 33 blocks are needed; the 33rd is computed only when a
 // chunk needs it.
 __device__ __forceinline__ void diag_stage_a(DiagStage &a, uint32_t op, bool inr, unsigned long long &ctr,
-                                             unsigned long long seed, unsigned long long stream,
-                                             unsigned long long nb, const int4 *__restrict__ bond_info,
-                                             unsigned lt, int lane) {
+                                             unsigned long long seed, unsigned long long stream, uint32_t nb,
+                                             const int4 *__restrict__ bond_info, unsigned lt, int lane) {
   const bool id = inr && op == 0u;
   const bool dg = inr && op != 0u && (op & 2u);
   const bool od = inr && op != 0u && !(op & 2u);
   const unsigned idm = __ballot_sync(FULL, id);
   const unsigned dgm = __ballot_sync(FULL, dg);
-  const unsigned long long tot = 2ull * __popc(idm) + __popc(dgm);
-  const unsigned long long d0 = ctr + 2ull * __popc(idm & lt) + __popc(dgm & lt);
+  const unsigned tot = 2u * __popc(idm) + __popc(dgm);
+  const unsigned long long d0 = ctr + 2u * __popc(idm & lt) + __popc(dgm & lt);
   const unsigned long long b0 = ctr >> 1;
-  a.op = op;
+  a.opb = op;
   a.kind = id ? 1 : dg ? 2 : od ? 3 : 0;
   a.u53 = 0;
-  a.bond = 0;
-  a.bi = make_int4(-1, -1, 0, 0);
   if (tot) {
     const uint4 x = philox_block(seed, stream, b0 + lane);
     uint4 x32 = make_uint4(0, 0, 0, 0);
@@ -413,19 +409,50 @@ __device__ __forceinline__ void diag_stage_a(DiagStage &a, uint32_t op, bool inr
       u2 = ((unsigned long long)blk1.y << 32) | blk1.x;
     }
     if (id) {
-      a.bond = (uint32_t)urange0(u1, nb);
+      a.opb = (uint32_t)urange0(u1, (unsigned long long)nb) << 11;
       a.u53 = u2 >> 11;
     } else if (dg) {
       a.u53 = u1 >> 11;
     }
   }
   ctr += tot;
-  if (dg || od) a.bond = op >> 11;
-  if (a.kind) a.bi = __ldg(bond_info + a.bond);
+  a.bi = a.kind ? __ldg(bond_info + (a.opb >> 11)) : make_int4(-1, -1, 0, 0);
+}
+
+// The exact test of one slot at operator count nj (src/sse.jl:150-186) in FP64, with the reference's
+// operations in its order: insertion of the diagonal vertex of weight index vo at an identity slot,
+// or removal of a diagonal operator.  Only the rare lanes the integer thresholds cannot classify get
+// here, so the two rates are recomputed (bit-identical IEEE divisions) instead of occupying registers
+// through the chunk loop (A/B at 4096 walkers of 32x32, beta = 16, with the 32-bit slot indices:
+// 201 instead of 230 cycles per slot under load).
+__device__ __forceinline__ bool diag_exact(const DevModel &M, const Chain &c, int L, int nj, bool insert,
+                                           unsigned long long u53, int vo) {
+  const double r = (double)u53 * 0x1.0p-53;
+  const double w = M.weight[vo];
+  if (insert) return r < __dmul_rn(__ddiv_rn(__ddiv_rn((double)M.nbonds, c.T), (double)(L - nj)), w);
+  return __dmul_rn(r, w) < __dmul_rn((double)(L - nj + 1), __ddiv_rn(c.T, (double)M.nbonds));
+}
+
+// Per-class integer thresholds for the window n_c +- 48, written by lane cls for class cls (lanes
+// below ncls): thr[2 cls] = (insert surely / insert never), thr[2 cls + 1] = (remove surely / never).
+__device__ __forceinline__ void diag_thresholds(const DevModel &M, const Chain &c, int L, int n_c,
+                                                ulonglong2 *thr, int lane) {
+  const double pmake_raw = __ddiv_rn((double)M.nbonds, c.T);
+  const double premove_raw = __ddiv_rn(c.T, (double)M.nbonds);
+  const double wc = M.cls_w[lane];
+  const int nlo = n_c - 48, nhi = n_c + 48;
+  const unsigned long long ti_a = thr_lt(__dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nlo)), wc));
+  const unsigned long long ti_r =
+      (L - nhi > 0) ? thr_lt(__dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nhi)), wc)) : U53_ALL;
+  const unsigned long long tr_a = thr_mul_lt(wc, __dmul_rn((double)(L - nhi + 1), premove_raw), 0ull);
+  const unsigned long long tr_r = thr_mul_lt(wc, __dmul_rn((double)(L - nlo + 1), premove_raw), U53_ALL);
+  thr[2 * lane] = make_ulonglong2(ti_a, ti_r);
+  thr[2 * lane + 1] = make_ulonglong2(tr_a, tr_r);
 }
 
 // thr: 1 KB of the warp's shared memory (the site table's, idle during this phase) for the per-class
-// thresholds: thr[2c] = (insert surely / insert never), thr[2c + 1] = (remove surely / remove never).
+// thresholds.  Slot indices, the cutoff and the operator count are 32-bit here: the engine keeps
+// opstrings below 2^29 slots.
 __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *__restrict__ ops, uint8_t *sst,
                                         ulonglong2 *thr, bool thermalized, long long &resize_count,
                                         long long &need_L, int lane) {
@@ -440,26 +467,22 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
     if (thermalized) resize_count++;
     __syncwarp();
   }
-  const double pmake_raw = (double)M.nbonds / c.T;
-  const double premove_raw = c.T / (double)M.nbonds;
   const unsigned lt = lanemask_lt();
-  const long long L = c.L;
-  long long n = c.n;
+  const int L = (int)c.L;
+  int n = (int)c.n;
   unsigned long long ctr = c.ctr;
-  const unsigned long long nb = (unsigned long long)M.nbonds;
+  const uint32_t nb = (uint32_t)M.nbonds;
   const unsigned long long seed = c.seed, stream = c.stream;
   const int4 *__restrict__ bond_info = M.bond_info;
   const DevType *__restrict__ types = M.types;
   const int32_t *__restrict__ diag_vc = M.diag_vc;
   const int8_t *__restrict__ vclass = M.vclass;
-  const double *__restrict__ weight = M.weight;
   const uint8_t *__restrict__ leg_state = M.leg_state;
   const int ncls = M.ncls;
   const bool use_thr = ncls <= 32;
-  const double wc = (use_thr && lane < ncls) ? M.cls_w[lane] : 0.0;
 
-  // per-class integer thresholds (in thr[], written by lane c for class c), valid while |n - n_c| <= 16
-  long long n_c = -(1ll << 60);
+  // per-class integer thresholds (in thr[]), valid while |n - n_c| <= 16
+  int n_c = -(1 << 30);
 
   // two chunks of opcodes in flight, the first chunk's stage A done before the loop
   uint32_t op_n1 = (lane < L) ? ops[lane] : 0u;
@@ -467,8 +490,8 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
   DiagStage cur;
   diag_stage_a(cur, op_n1, lane < L, ctr, seed, stream, nb, bond_info, lt, lane);
 
-  for (long long base = 0; base < L; base += 32) {
-    const long long p = base + lane;
+  for (int base = 0; base < L; base += 32) {
+    const int p = base + lane;
     // stage A of the next chunk and the opcode load two chunks ahead
     const uint32_t op_next = op_n2;
     op_n2 = (base + 64 + lane < L) ? ops[base + 64 + lane] : 0u;
@@ -483,7 +506,7 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
     const int si = cur.bi.x, sj = cur.bi.y, type = cur.bi.z;
     int vcode = -1, cls = -1, ups = 0;
     if (dg || od) {
-      vcode = (int)((cur.op >> 1) & 0x3FFu);
+      vcode = (int)((cur.opb >> 1) & 0x3FFu);
       const int vo = types[type].vert_off + (vcode >> 1);
       if (dg) cls = vclass[vo];
       else {
@@ -522,16 +545,7 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
     // thresholds for the window around n
     if (use_thr && (n - n_c > 16 || n_c - n > 16)) {
       n_c = n;
-      if (lane < ncls) {
-        const long long nlo = n_c - 48, nhi = n_c + 48;
-        const unsigned long long ti_a = thr_lt(__dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nlo)), wc));
-        const unsigned long long ti_r =
-            (L - nhi > 0) ? thr_lt(__dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nhi)), wc)) : U53_ALL;
-        const unsigned long long tr_a = thr_mul_lt(wc, __dmul_rn((double)(L - nhi + 1), premove_raw), 0ull);
-        const unsigned long long tr_r = thr_mul_lt(wc, __dmul_rn((double)(L - nlo + 1), premove_raw), U53_ALL);
-        thr[2 * lane] = make_ulonglong2(ti_a, ti_r);
-        thr[2 * lane + 1] = make_ulonglong2(tr_a, tr_r);
-      }
+      if (lane < ncls) diag_thresholds(M, c, L, n_c, thr, lane);
       __syncwarp();
     }
     // classify: surely accepted / surely rejected / maybe
@@ -540,34 +554,30 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
       ti = thr[2 * cls];
       tr = thr[2 * cls + 1];
     }
-    const unsigned long long a_ins = ti.x, r_ins = ti.y, a_rem = tr.x, r_rem = tr.y;
-    const long long nlo = n - __popc(dgm & lt);
-    const long long nhi = n + __popc(idm & lt);
+    const int nlo = n - __popc(dgm & lt);
+    const int nhi = n + __popc(idm & lt);
     bool alo = false, ahi = false;
     if (id) {
       if (cls < 0) {
         alo = ahi = false;  // invalid diagonal vertex: weight 0, never accepted
-      } else if (use_thr && cur.u53 < a_ins) {
+      } else if (use_thr && cur.u53 < ti.x) {
         alo = ahi = true;
-      } else if (use_thr && cur.u53 >= r_ins) {
+      } else if (use_thr && cur.u53 >= ti.y) {
         alo = ahi = false;
       } else {
-        const double r = (double)cur.u53 * 0x1.0p-53;
-        const double w = __ldg(weight + types[type].vert_off + (vcode >> 1));
-        alo = r < __dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nlo)), w);
-        ahi = r < __dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nhi)), w);
+        const int vo = types[type].vert_off + (vcode >> 1);
+        alo = diag_exact(M, c, L, nlo, true, cur.u53, vo);
+        ahi = diag_exact(M, c, L, nhi, true, cur.u53, vo);
       }
     } else if (dg) {
-      if (use_thr && cur.u53 < a_rem) {
+      if (use_thr && cur.u53 < tr.x) {
         alo = ahi = true;
-      } else if (use_thr && cur.u53 >= r_rem) {
+      } else if (use_thr && cur.u53 >= tr.y) {
         alo = ahi = false;
       } else {
-        const double r = (double)cur.u53 * 0x1.0p-53;
-        const double w = __ldg(weight + types[type].vert_off + (vcode >> 1));
-        const double rw = __dmul_rn(r, w);
-        alo = rw < __dmul_rn((double)(L - nlo + 1), premove_raw);
-        ahi = rw < __dmul_rn((double)(L - nhi + 1), premove_raw);
+        const int vo = types[type].vert_off + (vcode >> 1);
+        alo = diag_exact(M, c, L, nlo, false, cur.u53, vo);
+        ahi = diag_exact(M, c, L, nhi, false, cur.u53, vo);
       }
     }
     const bool amb = (id || dg) && (alo != ahi);
@@ -576,19 +586,14 @@ __device__ __noinline__ int diag_update(const DevModel &M, Chain &c, uint32_t *_
     for (unsigned am = __ballot_sync(FULL, amb); am; am &= am - 1) {
       const int j = __ffs(am) - 1;
       const unsigned below = (1u << j) - 1u;
-      const long long nj = n + __popc(plus & below) - __popc(minus & below);
+      const int nj = n + __popc(plus & below) - __popc(minus & below);
       bool acc = false;
-      if (lane == j) {
-        const double r = (double)cur.u53 * 0x1.0p-53;
-        const double w = __ldg(weight + types[type].vert_off + (vcode >> 1));
-        acc = id ? (r < __dmul_rn(__ddiv_rn(pmake_raw, (double)(L - nj)), w))
-                 : (__dmul_rn(r, w) < __dmul_rn((double)(L - nj + 1), premove_raw));
-      }
+      if (lane == j) acc = diag_exact(M, c, L, nj, id, cur.u53, types[type].vert_off + (vcode >> 1));
       const unsigned b = __ballot_sync(FULL, acc);
       if (idm & (1u << j)) plus |= b;
       else minus |= b;
     }
-    if ((plus >> lane) & 1u) ops[p] = 1u | ((uint32_t)vcode << 1) | (cur.bond << 11);
+    if ((plus >> lane) & 1u) ops[p] = 1u | ((uint32_t)vcode << 1) | (cur.opb & 0xFFFFF800u);
     if ((minus >> lane) & 1u) ops[p] = 0u;
     n += __popc(plus) - __popc(minus);
     __syncwarp();
