@@ -1,7 +1,8 @@
 """ctypes binding of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
 Used by ``tests/``, ``__graft_entry__.smoke()`` and the benchmark's CPU
-baseline as the checker.  The GPU engine never imports this module.
+baseline, to check results and to time the CPU path.  The GPU engine never
+imports this module.
 """
 
 from __future__ import annotations

@@ -45,7 +45,7 @@ def generate() -> str:
                           "%lanemask_lt read")
     dev = dev.replace("#pragma once", "")
     if "asm" in re.sub(r"//.*", "", dev).split():
-        raise RuntimeError("warp emulator build: sse_device.cuh has inline PTX this build does not emulate")
+        raise RuntimeError("warp emulator build: sse_device.cuh has inline PTX the emulator does not handle")
     eng = open(os.path.join(CSRC, "sse_engine.cu")).read()
     begin = eng.index("// ==== kernels: begin")
     end = eng.index("// ==== kernels: end ====")
