@@ -137,7 +137,10 @@ int sse_model_register(sse_engine *eng, const sse_model_desc *desc, int32_t *mod
  * then per estimator SignMag, SignAbsMag, SignMag2, SignMag4, SignMagChi) */
 int sse_model_nobs(sse_engine *eng, int32_t model_id, int32_t *nobs);
 
-/* ---- walkers: replaces MC(params) (src/sse.jl:26-45) ---- */
+/* ---- walkers: replaces MC(params) (src/sse.jl:26-45) ----
+ * Refuses (before allocating anything) T that is not positive and finite, negative warm-up sweeps or
+ * worm counts (SSE_ERR_ARG), and an initial cutoff whose opstring would reach 2^29 slots, the limit
+ * of the engine's 32-bit links and slot indices (SSE_ERR_CAPACITY). */
 int sse_walkers_create(sse_engine *eng, int32_t model_id, int32_t count, const sse_walker_params *params,
                        int32_t *ids);
 int sse_walkers_destroy(sse_engine *eng, int32_t count, const int32_t *ids);

@@ -1222,8 +1222,13 @@ int sse_walkers_create(sse_engine *e, int32_t model_id, int32_t count, const sse
   // all parameters are checked before anything is allocated
   for (int i = 0; i < count; i++) {
     const sse_walker_params &p = params[i];
-    if (!(p.T > 0) || p.diagonal_warmup_sweeps < 0 || !(p.init_num_worms >= 0))
+    if (!(p.T > 0) || !std::isfinite(p.T) || p.diagonal_warmup_sweeps < 0 || !(p.init_num_worms >= 0))
       return fail(e, SSE_ERR_ARG, "walker parameters out of range");
+    // links and slot indices are 32-bit: opstrings stay below 2^29 slots, the initial one included
+    const double cut0 = p.init_opstring_cutoff >= 0 ? (double)p.init_opstring_cutoff
+                                                    : std::nearbyint((double)e->models[model_id].nsites * p.T);
+    if (2.0 * cut0 + 163.0 >= (double)((1LL << 31) / 4))
+      return fail(e, SSE_ERR_CAPACITY, "initial opstring cutoff exceeds 2^29 slots");
   }
   const HostModel &hm = e->models[model_id];
   const size_t first = e->walkers.size();

@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 ARG = 1
+CAPACITY = 3
 
 
 @pytest.fixture
@@ -202,3 +203,24 @@ def test_noalloc_argument_and_limit_checks(S, fake):
         assert call(d=d) == code, field
     assert fake.fake_cuda_launches() == launches0
     assert call() == 0 and fake.fake_cuda_launches() > launches0
+
+
+def test_walker_creation_refuses_infinite_T_and_oversize_cutoffs(S, eng):
+    """Links and slot indices are 32-bit, so opstrings stay below 2^29 slots from creation on; an
+    infinite temperature (whose cutoff round(N*T) has no value) is refused like a non-positive one,
+    all before anything is allocated."""
+    from sse_gb300.engine import SSEError
+
+    mid = eng.register_model(square(S, 4))
+    for params, code in [
+        (dict(T=float("inf"), seed=1), ARG),
+        (dict(T=float("nan"), seed=1), ARG),
+        (dict(T=0.5, seed=1, init_opstring_cutoff=1 << 28), CAPACITY),
+        (dict(T=2.0 ** 40, seed=1), CAPACITY),  # round(16 T) far above 2^29
+    ]:
+        with pytest.raises(SSEError) as err:
+            eng.create_walkers(mid, [dict(T=0.5, seed=1), params])
+        assert err.value.code == code, params
+    # a cutoff that fits gets 2 c + 100 slots, rounded up to 64
+    (w,) = eng.create_walkers(mid, [dict(T=0.5, seed=1, init_opstring_cutoff=1000)]).tolist()
+    assert eng.info(w)["capacity"] >= 2100
