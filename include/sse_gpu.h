@@ -137,10 +137,15 @@ int sse_model_register(sse_engine *eng, const sse_model_desc *desc, int32_t *mod
  * then per estimator SignMag, SignAbsMag, SignMag2, SignMag4, SignMagChi) */
 int sse_model_nobs(sse_engine *eng, int32_t model_id, int32_t *nobs);
 
+/* A sweep runs ceil(num_worms) worms (src/sse.jl:195-198); creation, import and the allocation-free
+ * entry point refuse a worm count outside [0, SSE_MAX_WORMS_PER_SWEEP] with SSE_ERR_ARG. */
+#define SSE_MAX_WORMS_PER_SWEEP 2147483648.0 /* 2^31 */
+
 /* ---- walkers: replaces MC(params) (src/sse.jl:26-45) ----
- * Refuses (before allocating anything) T that is not positive and finite, negative warm-up sweeps or
- * worm counts (SSE_ERR_ARG), and an initial cutoff whose opstring would reach 2^29 slots, the limit
- * of the engine's 32-bit links and slot indices (SSE_ERR_CAPACITY). */
+ * Refuses (before allocating anything) T that is not positive and finite, negative warm-up sweeps,
+ * an initial worm count outside [0, SSE_MAX_WORMS_PER_SWEEP] (SSE_ERR_ARG), and an initial cutoff
+ * whose opstring would reach 2^29 slots, the limit of the engine's 32-bit links and slot indices
+ * (SSE_ERR_CAPACITY). */
 int sse_walkers_create(sse_engine *eng, int32_t model_id, int32_t count, const sse_walker_params *params,
                        int32_t *ids);
 int sse_walkers_destroy(sse_engine *eng, int32_t count, const int32_t *ids);
@@ -168,7 +173,9 @@ int sse_walker_info_get(sse_engine *eng, int32_t id, sse_walker_info *info);
 /* ops: at least info.L entries; state: nsites entries */
 int sse_walker_export(sse_engine *eng, int32_t id, uint32_t *ops, int64_t ops_len, uint8_t *state,
                       sse_walker_info *info);
-/* sets L, num_operators, sweeps, rng_counter, num_worms, avg_worm_length from info; capacity grows as needed */
+/* sets L, num_operators, sweeps, rng_counter, num_worms, avg_worm_length from info; capacity grows as needed.
+ * Refuses operators, spin states, num_worms outside [0, SSE_MAX_WORMS_PER_SWEEP] and a negative or
+ * infinite avg_worm_length with SSE_ERR_ARG, leaving the walker unchanged. */
 int sse_walker_import(sse_engine *eng, int32_t id, const uint32_t *ops, const uint8_t *state,
                       const sse_walker_info *info);
 

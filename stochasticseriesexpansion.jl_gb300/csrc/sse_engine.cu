@@ -1222,7 +1222,10 @@ int sse_walkers_create(sse_engine *e, int32_t model_id, int32_t count, const sse
   // all parameters are checked before anything is allocated
   for (int i = 0; i < count; i++) {
     const sse_walker_params &p = params[i];
-    if (!(p.T > 0) || !std::isfinite(p.T) || p.diagonal_warmup_sweeps < 0 || !(p.init_num_worms >= 0))
+    // worms per sweep: ceil(num_worms), so a count beyond 2^31 (or infinite) would keep one sweep
+    // running for hours
+    if (!(p.T > 0) || !std::isfinite(p.T) || p.diagonal_warmup_sweeps < 0 || !(p.init_num_worms >= 0) ||
+        !(p.init_num_worms <= SSE_MAX_WORMS_PER_SWEEP))
       return fail(e, SSE_ERR_ARG, "walker parameters out of range");
     // links and slot indices are 32-bit: opstrings stay below 2^29 slots, the initial one included
     const double cut0 = p.init_opstring_cutoff >= 0 ? (double)p.init_opstring_cutoff
@@ -1465,6 +1468,9 @@ int sse_walker_import(sse_engine *e, int32_t id, const uint32_t *ops, const uint
                       const sse_walker_info *info) {
   if (!e || !info || !valid_id(e, id) || (info->L > 0 && !ops) || !state) return SSE_ERR_ARG;
   if (info->L < 0 || info->num_operators < 0 || info->num_operators > info->L) return fail(e, SSE_ERR_ARG, "bad L/n");
+  if (!(info->num_worms >= 0) || !(info->num_worms <= SSE_MAX_WORMS_PER_SWEEP) || !(info->avg_worm_length >= 0) ||
+      !std::isfinite(info->avg_worm_length))
+    return fail(e, SSE_ERR_ARG, "worm controller state out of range");
   cudaSetDevice(e->device);
   const HostModel &hm = e->models[e->walkers[id].model];
   long long n = 0;
@@ -2013,7 +2019,10 @@ __global__ void k_noalloc_prep(NoAllocScratch *X, sse_model_desc d, sse_noalloc_
   // the walker's own state, read only once the tables it indexes are known to be valid
   const int phase = uw->phase;
   if (!s_bad && !s_unsup) {
-    if ((phase != PH_NEW && phase != PH_WARMUP && phase != PH_READY) || !(uw->T > 0.0) || !(uw->T < INFINITY)) {
+    const double nw = phase == PH_NEW ? uw->init_num_worms : uw->num_worms;
+    if ((phase != PH_NEW && phase != PH_WARMUP && phase != PH_READY) || !(uw->T > 0.0) || !(uw->T < INFINITY) ||
+        !(nw >= 0.0) || !(nw <= SSE_MAX_WORMS_PER_SWEEP) ||
+        (phase != PH_NEW && !(uw->avg_worm_length >= 0.0 && uw->avg_worm_length < INFINITY))) {
       s_bad = 1;
     } else if (phase != PH_NEW) {
       // a walker that went through (part of) Carlo.init! sweeps its own opstring and spin state

@@ -146,7 +146,9 @@ def test_noalloc_refuses_orphan_transition_row(S, emu):
 
 @pytest.mark.parametrize("case", ["warmup_L_past_capacity", "ready_L_past_capacity", "ready_n_past_L",
                                   "ready_bad_state", "ready_bad_operator_bond", "ready_bad_operator_vertex",
-                                  "phase_3", "phase_negative", "T_zero", "T_nan"])
+                                  "phase_3", "phase_negative", "T_zero", "T_nan", "ready_num_worms_huge",
+                                  "ready_num_worms_inf", "ready_avg_worm_length_negative",
+                                  "new_init_num_worms_inf"])
 def test_noalloc_refuses_bad_walker(S, emu, case):
     flat = square(S)
     c = Caller(S, emu, flat)
@@ -172,6 +174,15 @@ def test_noalloc_refuses_bad_walker(S, emu, case):
         w.T = 0.0
     elif case == "T_nan":
         w.T = float("nan")
+    elif case == "ready_num_worms_huge":  # a sweep runs ceil(num_worms) worms
+        w.num_worms = 2.0 ** 40
+    elif case == "ready_num_worms_inf":
+        w.num_worms = float("inf")
+    elif case == "ready_avg_worm_length_negative":
+        w.avg_worm_length = -1.0
+    elif case == "new_init_num_worms_inf":
+        w.phase = 0
+        w.init_num_worms = float("inf")
     before = c.chain()
     assert c.call() == ARG, case
     assert c.chain() == before

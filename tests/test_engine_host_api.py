@@ -224,3 +224,29 @@ def test_walker_creation_refuses_infinite_T_and_oversize_cutoffs(S, eng):
     # a cutoff that fits gets 2 c + 100 slots, rounded up to 64
     (w,) = eng.create_walkers(mid, [dict(T=0.5, seed=1, init_opstring_cutoff=1000)]).tolist()
     assert eng.info(w)["capacity"] >= 2100
+
+
+def test_worm_counts_out_of_range_are_refused(S, O, eng):
+    """A sweep runs ceil(num_worms) worms: an infinite or huge count (created or imported) would keep
+    one sweep on the GPU for hours, so both paths refuse it, and import leaves the walker as it was."""
+    from sse_gb300.engine import SSEError
+
+    flat = square(S, 4)
+    mid = eng.register_model(flat)
+    for nw in (float("inf"), float("nan"), -1.0, 2.0 ** 32):
+        with pytest.raises(SSEError) as err:
+            eng.create_walkers(mid, [dict(T=0.5, seed=1, init_num_worms=nw)])
+        assert err.value.code == ARG, nw
+    (wid,) = eng.create_walkers(mid, [dict(T=0.5, seed=21, stream=0)]).tolist()
+    w = oracle_chain(O, flat, 0.5, 20)
+    info = dict(num_operators=int(w.w.num_operators), rng_counter=int(w.w.ctr), num_worms=float(w.w.num_worms),
+                avg_worm_length=float(w.w.avg_worm_length), sweeps=int(w.w.sweeps))
+    eng.import_(wid, w.ops, w.state, info)
+    before = eng.info(wid)
+    for key, bad in (("num_worms", float("inf")), ("num_worms", 2.0 ** 40), ("avg_worm_length", float("nan")),
+                     ("avg_worm_length", -1.0)):
+        with pytest.raises(SSEError) as err:
+            eng.import_(wid, w.ops, w.state, dict(info, **{key: bad}))
+        assert err.value.code == ARG, (key, bad)
+    after = eng.info(wid)
+    assert after["num_worms"] == before["num_worms"] and after["avg_worm_length"] == before["avg_worm_length"]
